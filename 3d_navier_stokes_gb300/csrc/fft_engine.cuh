@@ -1,0 +1,223 @@
+// fft_engine.cuh — register-resident mixed-radix Stockham FFT for sm_103a.
+//
+// One length-N complex transform is spread over P = N/E threads; thread p
+// holds the E elements x[p + P*s], s < E, in registers. Each radix-R stage
+// does E/R butterflies per thread in registers; between stages the elements
+// are exchanged through shared memory (one write, one read per element).
+// The first stage's inputs come straight from global memory and the last
+// stage's outputs stay in registers in natural order (thread p holds
+// X[p + P*s]), so a kernel loads, transforms and stores with coalesced
+// accesses and only (stages - 1) shared-memory round trips.
+//
+// The index scheme is the Stockham autosort formulation used for GPU FFTs by
+// Govindaraju et al. (SC 2008): butterfly j of a stage with current sub-size
+// Ns reads x[j + r*N/R], twiddles by W_{Ns*R}^{r*(j mod Ns)} and writes
+// y[(j/Ns)*Ns*R + (j mod Ns) + r*Ns].
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace ns3d {
+
+template <typename T>
+struct __align__(2 * sizeof(T)) cx {
+    T x, y;
+};
+
+template <typename T> __device__ __forceinline__ cx<T> mk(T a, T b) { cx<T> r; r.x = a; r.y = b; return r; }
+template <typename T> __device__ __forceinline__ cx<T> operator+(cx<T> a, cx<T> b) { return mk(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ cx<T> operator-(cx<T> a, cx<T> b) { return mk(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ cx<T> operator*(cx<T> a, T s) { return mk(a.x * s, a.y * s); }
+template <typename T> __device__ __forceinline__ cx<T> cmul(cx<T> a, cx<T> b) {
+    return mk(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+template <typename T> __device__ __forceinline__ cx<T> conjg(cx<T> a) { return mk(a.x, -a.y); }
+template <typename T> __device__ __forceinline__ cx<T> mul_i(cx<T> a) { return mk(-a.y, a.x); }   // i*a
+template <typename T> __device__ __forceinline__ cx<T> mul_mi(cx<T> a) { return mk(a.y, -a.x); }  // -i*a
+template <typename T> __device__ __forceinline__ cx<T> czero() { return mk<T>(T(0), T(0)); }
+
+// read-only-path loads of a complex value
+__device__ __forceinline__ cx<float> ldg(const cx<float>* p) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    return mk(v.x, v.y);
+}
+__device__ __forceinline__ cx<double> ldg(const cx<double>* p) {
+    const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+    return mk(v.x, v.y);
+}
+
+// cos/sin of 2*pi*k/16 and 2*pi*k/12 (k < 16 / 12), the internal constants of
+// the radix-2..16 codelets.
+__device__ constexpr double kC16[16] = {
+    1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173,
+    0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613,
+    -1.0, -0.92387953251128675613, -0.70710678118654752440, -0.38268343236508977173,
+    0.0, 0.38268343236508977173, 0.70710678118654752440, 0.92387953251128675613};
+__device__ constexpr double kS16[16] = {
+    0.0, 0.38268343236508977173, 0.70710678118654752440, 0.92387953251128675613,
+    1.0, 0.92387953251128675613, 0.70710678118654752440, 0.38268343236508977173,
+    0.0, -0.38268343236508977173, -0.70710678118654752440, -0.92387953251128675613,
+    -1.0, -0.92387953251128675613, -0.70710678118654752440, -0.38268343236508977173};
+__device__ constexpr double kC12[12] = {
+    1.0, 0.86602540378443864676, 0.5, 0.0, -0.5, -0.86602540378443864676,
+    -1.0, -0.86602540378443864676, -0.5, 0.0, 0.5, 0.86602540378443864676};
+__device__ constexpr double kS12[12] = {
+    0.0, 0.5, 0.86602540378443864676, 1.0, 0.86602540378443864676, 0.5,
+    0.0, -0.5, -0.86602540378443864676, -1.0, -0.86602540378443864676, -0.5};
+
+// a * W_R^K with W_R = exp(-2 pi i / R); exact for the trivial angles.
+template <int R, int K, typename T>
+__device__ __forceinline__ cx<T> twc(cx<T> a) {
+    constexpr int k = K % R;
+    if constexpr (k == 0) {
+        return a;
+    } else if constexpr (4 * k == R) {
+        return mul_mi(a);
+    } else if constexpr (2 * k == R) {
+        return mk(-a.x, -a.y);
+    } else if constexpr (4 * k == 3 * R) {
+        return mul_i(a);
+    } else {
+        constexpr bool tri = (R % 3 == 0);
+        constexpr int idx = tri ? (k * 12 / R) : (k * 16 / R);
+        const T c = T(tri ? kC12[idx] : kC16[idx]);
+        const T s = T(tri ? kS12[idx] : kS16[idx]);
+        // (a.x + i a.y)(c - i s)
+        return mk(a.x * c + a.y * s, a.y * c - a.x * s);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Forward DFT codelets, in place on a[0..R-1] (natural order in and out).
+// Even sizes are split decimation-in-time into two halves.
+// ---------------------------------------------------------------------------
+template <int R, typename T> struct Dft;
+
+template <typename T> struct Dft<1, T> {
+    __device__ __forceinline__ static void run(cx<T>*) {}
+};
+template <typename T> struct Dft<2, T> {
+    __device__ __forceinline__ static void run(cx<T>* a) {
+        cx<T> t = a[0];
+        a[0] = t + a[1];
+        a[1] = t - a[1];
+    }
+};
+template <typename T> struct Dft<3, T> {
+    __device__ __forceinline__ static void run(cx<T>* a) {
+        const T h = T(0.86602540378443864676);
+        cx<T> s = a[1] + a[2], d = a[1] - a[2];
+        cx<T> m = a[0] - s * T(0.5);
+        a[0] = a[0] + s;
+        cx<T> jd = mk(d.y * h, -d.x * h);   // -i*sin(60)*d
+        a[1] = m + jd;
+        a[2] = m - jd;
+    }
+};
+template <typename T> struct Dft<4, T> {
+    __device__ __forceinline__ static void run(cx<T>* a) {
+        cx<T> s02 = a[0] + a[2], d02 = a[0] - a[2];
+        cx<T> s13 = a[1] + a[3], d13 = mul_mi(a[1] - a[3]);
+        a[0] = s02 + s13;
+        a[2] = s02 - s13;
+        a[1] = d02 + d13;
+        a[3] = d02 - d13;
+    }
+};
+
+template <int R, typename T, int K = 0>
+__device__ __forceinline__ void combine_half(cx<T>* e, cx<T>* o, cx<T>* a) {
+    if constexpr (K < R / 2) {
+        cx<T> t = twc<R, K>(o[K]);
+        a[K] = e[K] + t;
+        a[K + R / 2] = e[K] - t;
+        combine_half<R, T, K + 1>(e, o, a);
+    }
+}
+
+template <int R, typename T> struct Dft {
+    static_assert(R % 2 == 0, "odd codelet sizes other than 3 are not provided");
+    __device__ __forceinline__ static void run(cx<T>* a) {
+        cx<T> e[R / 2], o[R / 2];
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+            e[i] = a[2 * i];
+            o[i] = a[2 * i + 1];
+        }
+        Dft<R / 2, T>::run(e);
+        Dft<R / 2, T>::run(o);
+        combine_half<R, T>(e, o, a);
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Stage driver.
+//   v      : thread's E elements, v[s] = x[p + P*s] on entry, X[p + P*s] on exit
+//   sbuf   : exchange buffer; sidx(m) maps sequence index m to its slot
+//   tw     : table W_N^m = exp(-2 pi i m / N), m < N (read-only path)
+//   sync() : barrier over all threads sharing sbuf
+// Inverse transforms are computed as conj(DFT(conj(x))) by the callers.
+// ---------------------------------------------------------------------------
+template <typename T, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
+__device__ __forceinline__ void fft_stages(cx<T> (&v)[E], cx<T>* sbuf, int p,
+                                           const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
+    constexpr int P = N / E;
+    constexpr int Q = E / R;
+    constexpr bool last = (sizeof...(Rest) == 0);
+    static_assert(E % R == 0, "radix must divide the elements per thread");
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = p + q * P;
+        cx<T> a[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
+        int jm = 0;
+        if constexpr (Ns > 1) {
+            jm = j % Ns;
+            constexpr int step = N / (Ns * R);
+#pragma unroll
+            for (int r = 1; r < R; ++r) a[r] = cmul(a[r], ldg(&tw[r * jm * step]));
+        }
+        Dft<R, T>::run(a);
+        if constexpr (last) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];
+        } else {
+            const int idxD = (j / Ns) * Ns * R + jm;
+#pragma unroll
+            for (int r = 0; r < R; ++r) sbuf[sidx(idxD + r * Ns)] = a[r];
+        }
+    }
+    if constexpr (!last) {
+        sync();
+#pragma unroll
+        for (int s = 0; s < E; ++s) v[s] = sbuf[sidx(p + s * P)];
+        sync();
+        fft_stages<T, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
+    }
+}
+
+// A compile-time FFT plan: length N, E elements per thread, radices Rs...
+template <int N_, int E_, int... Rs>
+struct Plan {
+    static constexpr int N = N_;
+    static constexpr int E = E_;
+    static constexpr int P = N_ / E_;
+    static constexpr int nstages = sizeof...(Rs);
+    template <typename T, typename SIdx, typename Sync>
+    __device__ __forceinline__ static void fwd(cx<T> (&v)[E_], cx<T>* sbuf, int p,
+                                               const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
+        fft_stages<T, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+    }
+    template <typename T, typename SIdx, typename Sync>
+    __device__ __forceinline__ static void inv(cx<T> (&v)[E_], cx<T>* sbuf, int p,
+                                               const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
+#pragma unroll
+        for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
+        fft_stages<T, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+#pragma unroll
+        for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
+    }
+};
+
+}  // namespace ns3d

@@ -1,0 +1,66 @@
+// ns3d_base.h — type-erased engine interface behind the C ABI. One concrete
+// engine exists per (precision, grid size); see ns3d_impl.cuh.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/ns3d.h"
+
+namespace ns3d {
+
+class Base {
+  public:
+    Base(const ns3d_params& p, cudaStream_t s) : p_(p), s_(s) { err_[0] = 0; }
+    virtual ~Base() {}
+    virtual ns3d_status init() = 0;
+    virtual int kernels_per_step() const = 0;
+    virtual ns3d_status step(int nsteps) = 0;
+    virtual ns3d_status step_host(const double* in, double* out) = 0;
+    virtual ns3d_status last_step_ms(float* ms) = 0;
+    virtual ns3d_status profile(int reps, const char** names, float* ms, double* bytes, int maxc, int* count) = 0;
+    virtual ns3d_status rhs_host(const double* in, double* out) = 0;
+    virtual ns3d_status set_state_host(const double* u) = 0;
+    virtual ns3d_status get_state_host(double* u) = 0;
+    virtual ns3d_status measurables(ns3d_measures* m, double* Ek, double* Ok) = 0;
+    virtual ns3d_status ic_real(int kind) = 0;
+    virtual ns3d_status ic_spectrum(uint64_t seed, double k0, double energy) = 0;
+    virtual ns3d_status ic_host(const double* u) = 0;
+    virtual ns3d_status ic_zero() = 0;
+    virtual ns3d_status real_space_host(double* u, double* w) = 0;
+    virtual ns3d_status max_speed_sum(double* umax) = 0;
+    virtual ns3d_status get_time(double* t, double* dt, long* iters) = 0;
+    virtual ns3d_status set_time(double t, double dt, long iters) = 0;
+    virtual ns3d_status get_forcing_target(double* e) = 0;
+    virtual ns3d_status set_forcing_target(double e) = 0;
+    virtual void* state_ptr() = 0;
+
+    const char* err() const { return err_; }
+    void set_err(const char* fmt, ...) {
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(err_, sizeof(err_), fmt, ap);
+        va_end(ap);
+    }
+    cudaStream_t stream() const { return s_; }
+
+  protected:
+    ns3d_params p_;
+    cudaStream_t s_;
+    char err_[512];
+};
+
+// Factories, one per precision (ns3d_inst_f32.cu / ns3d_inst_f64.cu).
+Base* make_f32(int N, const ns3d_params& p, cudaStream_t s);
+Base* make_f64(int N, const ns3d_params& p, cudaStream_t s);
+bool supported_n(int N);
+
+inline unsigned long long host_splitmix64(unsigned long long x) {
+    unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+}  // namespace ns3d

@@ -1,0 +1,524 @@
+// ns3d_impl.cuh — host-side engine for one (precision, grid size): device
+// memory plan, pass launches, CUDA-graph capture of a whole time step,
+// diagnostics, initial conditions and layout conversion.
+#pragma once
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "ns3d_base.h"
+#include "ns3d_kernels.cuh"
+
+namespace ns3d {
+
+#define NS3D_CK(call)                                                        \
+    do {                                                                     \
+        cudaError_t e_ = (call);                                             \
+        if (e_ != cudaSuccess) {                                             \
+            set_err("%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+            return NS3D_ERR_CUDA;                                            \
+        }                                                                    \
+    } while (0)
+
+// e^{-2 pi i m / n} with the quarter-turn reduction used by the transforms.
+void twiddle_table(int n, double* re, double* im);
+
+template <typename T, int N>
+class Impl final : public Base {
+    using G = Geo<N>;
+    using PA = typename Plans<N>::A;
+    using PX = typename Plans<N>::X;
+    static constexpr int TA = tile_a<T, N>();
+    static constexpr int TX = tile_x<T, N>();
+    static constexpr int ZP = zpairs<N>();
+    static constexpr int NTA = (G::NZ1 + TA - 1) / TA;
+    static constexpr int NTX = (G::NZ1 + TX - 1) / TX;
+    static constexpr int LPC = meas_lines_per_cta<N>();
+    static constexpr long long NMEAS = ((long long)N * G::NKY + LPC - 1) / LPC;
+    static constexpr int MWIDTH = 5 + 2 * G::NSP;
+
+  public:
+    Impl(const ns3d_params& p, cudaStream_t s) : Base(p, s) {}
+
+    ~Impl() override {
+        if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
+        for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
+                        (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_})
+            if (q) cudaFree(q);
+        if (sd_host_) cudaFreeHost(sd_host_);
+        if (mout_host_) cudaFreeHost(mout_host_);
+        if (ev0_) cudaEventDestroy(ev0_);
+        if (ev1_) cudaEventDestroy(ev1_);
+    }
+
+    int kernels_per_step() const override { return 4 * 5 + (p_.cfl > 0 ? 1 : 0) + 1; }
+
+    ns3d_status init() override {
+        const size_t fb = sizeof(cx<T>) * (size_t)G::FS;
+        NS3D_CK(cudaMalloc(&U_, 3 * fb));
+        NS3D_CK(cudaMalloc(&UT_, 3 * fb));
+        NS3D_CK(cudaMalloc(&ACC_, 3 * fb));
+        NS3D_CK(cudaMalloc(&W_, 6 * fb));
+        NS3D_CK(cudaMemsetAsync(U_, 0, 3 * fb, s_));
+        NS3D_CK(cudaMemsetAsync(UT_, 0, 3 * fb, s_));
+        NS3D_CK(cudaMemsetAsync(ACC_, 0, 3 * fb, s_));
+        NS3D_CK(cudaMalloc(&tw_, sizeof(cx<T>) * N));
+        NS3D_CK(cudaMalloc(&tab_, sizeof(cx<T>) * (G::KC2 + 1)));
+        NS3D_CK(cudaMalloc(&part_, sizeof(double) * NMEAS * MWIDTH));
+        NS3D_CK(cudaMalloc(&mout_, sizeof(double) * MWIDTH));
+        NS3D_CK(cudaMallocHost(&mout_host_, sizeof(double) * MWIDTH));
+        NS3D_CK(cudaMalloc(&sd_, sizeof(StepDev)));
+        NS3D_CK(cudaMallocHost(&sd_host_, sizeof(StepDev)));
+        NS3D_CK(cudaEventCreate(&ev0_));
+        NS3D_CK(cudaEventCreate(&ev1_));
+        // twiddles
+        std::vector<double> re(N), im(N);
+        twiddle_table(N, re.data(), im.data());
+        std::vector<cx<T>> h(N);
+        for (int m = 0; m < N; ++m) { h[m].x = T(re[m]); h[m].y = T(im[m]); }
+        NS3D_CK(cudaMemcpyAsync(tw_, h.data(), sizeof(cx<T>) * N, cudaMemcpyHostToDevice, s_));
+        // step state
+        StepDev sd{};
+        sd.t = p_.t0; sd.dt = p_.dt; sd.t0 = p_.t0; sd.nu = p_.nu; sd.cfl = p_.cfl;
+        *sd_host_ = sd;
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        // opt-in shared memory sizes
+        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
+        NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
+        NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
+        set_xfwd_attrs<INT_IFRK4>();
+        set_xfwd_attrs<INT_RK4CN>();
+        ns3d_status st = refresh_tables();
+        if (st != NS3D_OK) return st;
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+
+    // ---------------------------------------------------------------- passes
+    static constexpr size_t smem_a() { return sizeof(cx<T>) * (size_t)N * TA; }
+    static constexpr size_t smem_x() { return sizeof(cx<T>) * (size_t)N * TX; }
+    static constexpr size_t smem_z() {
+        return sizeof(cx<T>) * (size_t)ZP * 3 * zpad<N>() + sizeof(T) * (size_t)ZP * 12 * N;
+    }
+
+    template <int INTEG>
+    void set_xfwd_attrs() {
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_RHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+    }
+
+    void p1(const cx<T>* in) {
+        k_xinv<T, N><<<dim3(NTA, G::NKY), TA * PA::P, smem_a(), s_>>>(in, W_, tw_);
+    }
+    void p2() { k_ypass<T, N, true><<<dim3(NTA, N, 6), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
+    void p3(int want_umax) {
+        k_zpass<T, N, 0><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            W_, tw_, nullptr, &sd_->umax_bits, want_umax);
+    }
+    void p4() { k_ypass<T, N, false><<<dim3(NTA, N, 3), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
+    template <int INTEG, int MODE>
+    void p5x(cx<T>* out) {
+        k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY), TX * PX::P, smem_x(), s_>>>(
+            W_, U_, UT_, out ? out : ACC_, tw_, sd_, tab_);
+    }
+    template <int MODE>
+    void p5(cx<T>* out = nullptr) {
+        if (p_.integrator == INT_RK4CN) p5x<INT_RK4CN, MODE>(out);
+        else p5x<INT_IFRK4, MODE>(out);
+    }
+    void tables(int use_cfl) {
+        const int n = G::KC2 + 1;
+        k_tables<T, N><<<(n + 255) / 256, 256, 0, s_>>>(tab_, sd_, p_.integrator, p_.visc_pow, use_cfl);
+    }
+
+    // one time step = 4 nonlinear evaluations with fused stage epilogues
+    void launch_step() {
+        const int cfl = p_.cfl > 0 ? 1 : 0;
+        p1(U_); p2(); p3(cfl);
+        if (cfl) tables(1);
+        p4(); p5<X_STAGE1>();
+        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE2>();
+        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE3>();
+        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE4>();
+        k_step_end<T, N><<<1, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+    }
+
+    ns3d_status build_graph() {
+        if (graph_exec_) return NS3D_OK;
+        cudaGraph_t g = nullptr;
+        NS3D_CK(cudaStreamBeginCapture(s_, cudaStreamCaptureModeThreadLocal));
+        launch_step();
+        cudaError_t e = cudaStreamEndCapture(s_, &g);
+        if (e != cudaSuccess) {
+            set_err("graph capture: %s", cudaGetErrorString(e));
+            return NS3D_ERR_CUDA;
+        }
+        e = cudaGraphInstantiate(&graph_exec_, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            set_err("graph instantiate: %s", cudaGetErrorString(e));
+            graph_exec_ = nullptr;
+            return NS3D_ERR_CUDA;
+        }
+        return NS3D_OK;
+    }
+
+    ns3d_status step(int nsteps) override {
+        if (nsteps <= 0) return NS3D_OK;
+        ns3d_status st = build_graph();
+        if (st != NS3D_OK) return st;
+        NS3D_CK(cudaEventRecord(ev0_, s_));
+        for (int k = 0; k < nsteps; ++k) NS3D_CK(cudaGraphLaunch(graph_exec_, s_));
+        NS3D_CK(cudaEventRecord(ev1_, s_));
+        return check_status();
+    }
+
+    ns3d_status check_status() {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        NS3D_CK(cudaGetLastError());
+        if (sd_host_->status != 0) {
+            set_err("numeric health check failed at step %lld (NaN/Inf energy or speed)", sd_host_->iters);
+            return NS3D_ERR_NUMERIC;
+        }
+        return NS3D_OK;
+    }
+
+    ns3d_status last_step_ms(float* ms) override {
+        NS3D_CK(cudaEventElapsedTime(ms, ev0_, ev1_));
+        return NS3D_OK;
+    }
+
+    // per-kernel-class timing of `reps` steps launched one kernel at a time
+    ns3d_status profile(int reps, const char** names, float* ms, double* bytes, int maxc, int* count) override {
+        static const char* kNames[6] = {"k_xinv", "k_ypass_inv", "k_zpass", "k_ypass_fwd", "k_xfwd", "k_misc"};
+        std::vector<cudaEvent_t> ev(2 * 6 * 4 + 2);
+        for (auto& e : ev) NS3D_CK(cudaEventCreate(&e));
+        double acc[6] = {0, 0, 0, 0, 0, 0};
+        const int cfl = p_.cfl > 0 ? 1 : 0;
+        for (int r = 0; r < reps; ++r) {
+            int q = 0;
+            for (int s = 0; s < 4; ++s) {
+                const cx<T>* in = s == 0 ? U_ : UT_;
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p1(in);
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p2();
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p3(s == 0 ? cfl : 0);
+                if (s == 0 && cfl) tables(1);
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p4();
+                NS3D_CK(cudaEventRecord(ev[q++], s_));
+                if (s == 0) p5<X_STAGE1>(); else if (s == 1) p5<X_STAGE2>(); else if (s == 2) p5<X_STAGE3>(); else p5<X_STAGE4>();
+                NS3D_CK(cudaEventRecord(ev[q++], s_));
+            }
+            k_step_end<T, N><<<1, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+            NS3D_CK(cudaEventRecord(ev[q++], s_));
+            NS3D_CK(cudaStreamSynchronize(s_));
+            q = 0;
+            for (int s = 0; s < 4; ++s) {
+                for (int k = 0; k < 5; ++k) {
+                    float t = 0;
+                    NS3D_CK(cudaEventElapsedTime(&t, ev[q + k], ev[q + k + 1]));
+                    acc[k] += t;
+                }
+                q += 6;
+            }
+            float t = 0;
+            NS3D_CK(cudaEventElapsedTime(&t, ev[q - 1], ev[q]));
+            acc[5] += t;
+        }
+        for (auto& e : ev) cudaEventDestroy(e);
+        // compulsory bytes per launch (loads of non-zero inputs + stores of needed outputs)
+        const double w = (double)sizeof(cx<T>);
+        const double sph = sphere_modes(), circ = circle_cols(), full = (double)N * N * G::NZ1;
+        const double b[6] = {
+            w * (3 * sph + 6 * circ),               // P1: u_hat in, 6 fields on the (x, ky^2+kz^2<=KC^2) set
+            w * (6 * circ + 6 * full),              // P2
+            w * (6 * full + 3 * full),              // P3
+            w * (3 * full + 3 * circ),              // P4
+            w * (3 * circ + 9.75 * sph),            // P5: 3 fields in + state (mean over the 4 stages)
+            0.0};
+        int n = 0;
+        for (int k = 0; k < 6 && n < maxc; ++k, ++n) {
+            names[n] = kNames[k];
+            ms[n] = (float)(acc[k] / reps / (k == 5 ? 1 : 4));
+            if (bytes) bytes[n] = b[k];
+        }
+        *count = n;
+        return check_status();
+    }
+    double sphere_modes() const {   // modes with kz >= 0 inside the sphere
+        double c = 0;
+        for (int kx = -G::KC; kx <= G::KC; ++kx)
+            for (int ky = -G::KC; ky <= G::KC; ++ky) {
+                const int r = G::KC2 - kx * kx - ky * ky;
+                if (r >= 0) c += std::floor(std::sqrt((double)r) + 1e-9) + 1;
+            }
+        return c;
+    }
+    double circle_cols() const {   // (x, ky, kz) with ky^2 + kz^2 <= KC^2
+        double c = 0;
+        for (int ky = -G::KC; ky <= G::KC; ++ky) c += std::floor(std::sqrt((double)(G::KC2 - ky * ky)) + 1e-9) + 1;
+        return c * N;
+    }
+
+    // --------------------------------------------------------------- rhs
+    ns3d_status rhs_host(const double* in, double* out) override {
+        ns3d_status st = upload(in, UT_);
+        if (st != NS3D_OK) return st;
+        p1(UT_); p2(); p3(0); p4(); p5<X_RHS>(ACC_);
+        return download(ACC_, out);
+    }
+
+    // ----------------------------------------------------- state transfer
+    ns3d_status ensure_stage() {
+        if (!stage_) NS3D_CK(cudaMalloc(&stage_, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1)));
+        return NS3D_OK;
+    }
+    ns3d_status upload(const double* host, cx<T>* dst) {
+        ns3d_status st = ensure_stage();
+        if (st != NS3D_OK) return st;
+        NS3D_CK(cudaMemcpyAsync(stage_, host, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1),
+                                cudaMemcpyHostToDevice, s_));
+        k_pack<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(stage_, dst);
+        NS3D_CK(cudaGetLastError());
+        return NS3D_OK;
+    }
+    ns3d_status download(const cx<T>* src, double* host) {
+        ns3d_status st = ensure_stage();
+        if (st != NS3D_OK) return st;
+        k_unpack<T, N><<<grid_for((long long)N * N * (N / 2 + 1)), 256, 0, s_>>>(src, stage_);
+        NS3D_CK(cudaMemcpyAsync(host, stage_, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1),
+                                cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        NS3D_CK(cudaGetLastError());
+        return NS3D_OK;
+    }
+    static unsigned grid_for(long long n) {
+        long long g = (n + 255) / 256;
+        if (g > 152 * 32) g = 152 * 32;
+        return (unsigned)(g < 1 ? 1 : g);
+    }
+
+    ns3d_status set_state_host(const double* u) override {
+        ns3d_status st = upload(u, U_);
+        if (st != NS3D_OK) return st;
+        return reset_forcing_target();
+    }
+    ns3d_status get_state_host(double* u) override { return download(U_, u); }
+
+    ns3d_status step_host(const double* in, double* out) override {
+        ns3d_status st;
+        if (in && (st = upload(in, U_)) != NS3D_OK) return st;
+        if ((st = build_graph()) != NS3D_OK) return st;
+        NS3D_CK(cudaGraphLaunch(graph_exec_, s_));
+        if (out) {
+            if ((st = download(U_, out)) != NS3D_OK) return st;
+        }
+        return check_status();
+    }
+
+    // -------------------------------------------------------- diagnostics
+    ns3d_status measure_dev(const cx<T>* u) {
+        k_measure<T, N><<<(unsigned)NMEAS, MEAS_WARPS * 32, 0, s_>>>(u, p_.nu, p_.visc_pow, part_);
+        const double N3 = (double)N * N * N;
+        k_measure_reduce<<<(MWIDTH + 127) / 128, 128, 0, s_>>>(part_, (int)NMEAS, MWIDTH, G::NSP, N3 * N3, mout_);
+        NS3D_CK(cudaMemcpyAsync(mout_host_, mout_, sizeof(double) * MWIDTH, cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        NS3D_CK(cudaGetLastError());
+        return NS3D_OK;
+    }
+    ns3d_status measurables(ns3d_measures* m, double* Ek, double* Ok) override {
+        ns3d_status st = measure_dev(U_);
+        if (st != NS3D_OK) return st;
+        if (m) {
+            m->energy = mout_host_[0];
+            m->enstrophy = mout_host_[1];
+            m->palinstrophy = mout_host_[2];
+            m->helicity = mout_host_[3];
+            m->dissipation = mout_host_[4];
+        }
+        const int ns = n_spect();
+        for (int b = 0; b < ns; ++b) {
+            if (Ek) Ek[b] = b < G::NSP ? mout_host_[5 + b] : 0.0;
+            if (Ok) Ok[b] = b < G::NSP ? mout_host_[5 + G::NSP + b] : 0.0;
+        }
+        return NS3D_OK;
+    }
+    int n_spect() const { return (int)std::sqrt(3.0 * ((double)N / 2.0) * ((double)N / 2.0)) + 1; }
+
+    // ------------------------------------------------- initial conditions
+    ns3d_status ensure_real() {
+        if (!real_) NS3D_CK(cudaMalloc(&real_, sizeof(T) * 6 * (size_t)N * N * N));
+        return NS3D_OK;
+    }
+    ns3d_status ic_real(int kind) override {
+        ns3d_status st = ensure_real();
+        if (st != NS3D_OK) return st;
+        k_fill_real<T, N><<<grid_for((long long)N * N * N), 256, 0, s_>>>(real_, kind);
+        k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            W_, tw_, real_, nullptr, 0);
+        p4();
+        p5<X_PLAIN>(U_);
+        NS3D_CK(cudaGetLastError());
+        return finish_ic();
+    }
+    ns3d_status ic_spectrum(uint64_t seed, double k0, double energy) override {
+        unsigned long long key = host_splitmix64(seed);
+        k_spectrum_ic<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(U_, key, k0);
+        ns3d_status st = measure_dev(U_);
+        if (st != NS3D_OK) return st;
+        const double e = mout_host_[0];
+        const double target = 8.0 * M_PI * M_PI * M_PI * energy;
+        if (e > 0.0) k_scale<T, N><<<grid_for(3 * G::FS), 256, 0, s_>>>(U_, std::sqrt(target / e));
+        NS3D_CK(cudaGetLastError());
+        return finish_ic();
+    }
+    ns3d_status ic_host(const double* u) override {
+        ns3d_status st = upload(u, U_);
+        if (st != NS3D_OK) return st;
+        return finish_ic();
+    }
+    ns3d_status ic_zero() override {
+        NS3D_CK(cudaMemsetAsync(U_, 0, sizeof(cx<T>) * 3 * (size_t)G::FS, s_));
+        return finish_ic();
+    }
+    ns3d_status finish_ic() {
+        ns3d_status st = set_time(p_.t0, p_.dt, 0);
+        if (st != NS3D_OK) return st;
+        return reset_forcing_target();
+    }
+    ns3d_status reset_forcing_target() {
+        if (p_.forcing != 1) return NS3D_OK;
+        double e = 0;
+        ns3d_status st = shell_energy(&e);
+        if (st != NS3D_OK) return st;
+        return set_forcing_target(e);
+    }
+    // energy of shells 1 <= round(|k|) <= force_k, FP64, from the spectrum
+    ns3d_status shell_energy(double* e) {
+        ns3d_status st = measure_dev(U_);
+        if (st != NS3D_OK) return st;
+        double s = 0;
+        for (int b = 1; b <= p_.force_k && b < G::NSP; ++b) s += mout_host_[5 + b];
+        *e = s;
+        return NS3D_OK;
+    }
+
+    // ------------------------------------------------------- real space
+    ns3d_status real_space_host(double* u, double* w) override {
+        ns3d_status st = ensure_real();
+        if (st != NS3D_OK) return st;
+        double* du = nullptr;
+        size_t rb = sizeof(double) * 3 * (size_t)N * N * (N + 2);
+        NS3D_CK(cudaMalloc(&du, 2 * rb));
+        p1(U_); p2();
+        k_zpass<T, N, 1><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            W_, tw_, real_, nullptr, 0);
+        k_real_unpack<T, N><<<grid_for((long long)N * N * (N + 2)), 256, 0, s_>>>(real_, du, du + rb / sizeof(double));
+        cudaError_t e = cudaGetLastError();
+        if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, du, rb, cudaMemcpyDeviceToHost, s_);
+        if (e == cudaSuccess && w) e = cudaMemcpyAsync(w, du + rb / sizeof(double), rb, cudaMemcpyDeviceToHost, s_);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+        cudaFree(du);
+        if (e != cudaSuccess) {
+            set_err("real_space: %s", cudaGetErrorString(e));
+            return NS3D_ERR_CUDA;
+        }
+        return NS3D_OK;
+    }
+
+    ns3d_status max_speed_sum(double* umax) override {
+        NS3D_CK(cudaMemsetAsync(&sd_->umax_bits, 0, sizeof(unsigned long long), s_));
+        p1(U_); p2(); p3(1);
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        const unsigned long long b = sd_host_->umax_bits;
+        if (sizeof(T) == 4) {
+            unsigned u32 = (unsigned)b;
+            float f;
+            std::memcpy(&f, &u32, 4);
+            *umax = f;
+        } else {
+            double d;
+            std::memcpy(&d, &b, 8);
+            *umax = d;
+        }
+        NS3D_CK(cudaMemsetAsync(&sd_->umax_bits, 0, sizeof(unsigned long long), s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+
+    // ------------------------------------------------------ bookkeeping
+    ns3d_status refresh_tables() {
+        tables(0);
+        NS3D_CK(cudaGetLastError());
+        return NS3D_OK;
+    }
+    ns3d_status get_time(double* t, double* dt, long* iters) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        if (t) *t = sd_host_->t;
+        if (dt) *dt = sd_host_->dt;
+        if (iters) *iters = (long)sd_host_->iters;
+        return NS3D_OK;
+    }
+    ns3d_status set_time(double t, double dt, long iters) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        sd_host_->t = t;
+        sd_host_->dt = dt;
+        sd_host_->iters = iters;
+        sd_host_->t0 = t - (p_.cfl > 0 ? 0.0 : (double)iters * dt);
+        sd_host_->umax_bits = 0;
+        sd_host_->status = 0;
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        ns3d_status st = refresh_tables();
+        if (st != NS3D_OK) return st;
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+    ns3d_status get_forcing_target(double* e) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        *e = sd_host_->force_target;
+        return NS3D_OK;
+    }
+    ns3d_status set_forcing_target(double e) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        sd_host_->force_target = e;
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+
+    // device pointers for in-library tools
+    void* state_ptr() override { return U_; }
+
+  private:
+    cx<T>* U_ = nullptr;
+    cx<T>* UT_ = nullptr;
+    cx<T>* ACC_ = nullptr;
+    cx<T>* W_ = nullptr;
+    cx<T>* tw_ = nullptr;
+    cx<T>* tab_ = nullptr;
+    double* part_ = nullptr;
+    double* mout_ = nullptr;
+    double* mout_host_ = nullptr;
+    double2* stage_ = nullptr;
+    T* real_ = nullptr;
+    StepDev* sd_ = nullptr;
+    StepDev* sd_host_ = nullptr;
+    cudaGraphExec_t graph_exec_ = nullptr;
+    cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+};
+
+}  // namespace ns3d

@@ -1,0 +1,877 @@
+// ns3d_kernels.cuh — CUDA kernels of the hot path (templated on precision T
+// and grid size N; instantiated in ns3d_inst_*.cu).
+//
+// Device layout. Every Fourier quantity is stored per component as
+// complex [N (x or kx)][N (y or ky)][NZP (kz)] with only kz <= KC = N/3 used
+// (NZP = KC+1 rounded up to 8). The 2/3 rule zeroes every mode with
+// |k| > N/3 (solver.c:1709-1756), so the Nyquist plane and all modes outside
+// the dealiasing sphere are never stored, loaded or transformed: loads of
+// known-zero inputs are predicated off and stores of outputs that the next
+// pass never reads are skipped.
+//
+// One nonlinear-term evaluation N(u) (NonlinearRHSBatch, solver.c:620-731)
+// is five passes over HBM:
+//   P1 k_xinv  : inverse FFT along kx of u_hat with the curl w_hat = i k x u_hat
+//                formed on load (solver.c:637-650); 3 fields in, 6 out.
+//   P2 k_ypass : inverse FFT along ky (6 fields, in place).
+//   P3 k_zpass : per z line: c2r of the 6 fields (two real lines per complex
+//                FFT), u x w in shared memory (solver.c:664-677), r2c of the 3
+//                products; in place. Also max(|u|+|v|+|w|) for the CFL step.
+//   P4 k_ypass : forward FFT along y (3 fields, in place).
+//   P5 k_xfwd  : forward FFT along x, then per mode the Leray projection
+//                (solver.c:689-721), the dealias mask and the RK stage
+//                algebra, written straight into the integrator's arrays.
+// The inverse passes scale by 1/N^3 on load, so real-space fields are the true
+// velocity/vorticity and the forward transform yields the reference's
+// FFT(u x w)/N^6 directly.
+#pragma once
+#include "fft_engine.cuh"
+
+namespace ns3d {
+
+// ---------------------------------------------------------------------------
+// Geometry and FFT plans
+// ---------------------------------------------------------------------------
+template <int N_>
+struct Geo {
+    static constexpr int N = N_;
+    static constexpr int KC = N_ / 3;               // dealias radius, integer N/3 (solver.c:1732)
+    static constexpr int KC2 = KC * KC;
+    static constexpr int NZ1 = KC + 1;              // kz columns in use
+    static constexpr int NZP = (NZ1 + 7) / 8 * 8;   // stored kz columns
+    static constexpr long long FS = (long long)N_ * N_ * NZP;   // elements per field
+    static constexpr int NKY = 2 * KC + 1;          // ky rows with |ky| <= KC
+    static constexpr int NSP = KC + 1;              // spectrum bins that can be non-zero
+};
+
+// wavenumber of storage index i (InitializeSpaceVariables, solver.c:1786-1812)
+template <int N> __device__ __forceinline__ int kof(int i) { return i <= N / 2 ? i : i - N; }
+
+template <int N> struct Plans;
+template <> struct Plans<8>    { using A = Plan<8, 8, 8>;            using X = A; };
+template <> struct Plans<16>   { using A = Plan<16, 16, 16>;         using X = A; };
+template <> struct Plans<24>   { using A = Plan<24, 12, 12, 2>;      using X = A; };
+template <> struct Plans<32>   { using A = Plan<32, 8, 4, 8>;        using X = A; };
+template <> struct Plans<48>   { using A = Plan<48, 12, 4, 12>;     using X = A; };
+template <> struct Plans<64>   { using A = Plan<64, 8, 8, 8>;        using X = A; };
+template <> struct Plans<96>   { using A = Plan<96, 12, 4, 4, 6>;    using X = A; };
+template <> struct Plans<128>  { using A = Plan<128, 16, 16, 8>;     using X = Plan<128, 8, 8, 4, 4>; };
+template <> struct Plans<256>  { using A = Plan<256, 16, 16, 16>;    using X = Plan<256, 8, 8, 8, 4>; };
+template <> struct Plans<512>  { using A = Plan<512, 16, 8, 8, 8>;   using X = Plan<512, 8, 8, 8, 8>; };
+template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = Plan<1024, 8, 8, 8, 4, 4>; };
+
+// Tile width (pencils per CTA along kz) of the strided passes: one 128-byte
+// row segment per pencil row where the thread count allows.
+template <typename T, int N> constexpr int tile_a() {
+    return sizeof(T) == 4 ? (Plans<N>::A::P * 16 <= 512 ? 16 : 8) : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
+}
+template <typename T, int N> constexpr int tile_x() {
+    return sizeof(T) == 4 ? (Plans<N>::X::P * 16 <= 512 ? 16 : 8) : (Plans<N>::X::P * 8 <= 256 ? 8 : 4);
+}
+// line pairs per CTA of the z pass (>= 96 threads)
+template <int N> constexpr int zpairs() {
+    return (3 * Plans<N>::A::P >= 96) ? 1 : (96 + 3 * Plans<N>::A::P - 1) / (3 * Plans<N>::A::P);
+}
+
+struct SyncBlock {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+template <int TT>
+struct StridedIdx {   // exchange slot of element m of pencil t: [m][TT]
+    int t;
+    __device__ __forceinline__ int operator()(int m) const { return m * TT + t; }
+};
+struct PaddedIdx {    // exchange slot of element m of one line: one pad slot per 16
+    __device__ __forceinline__ int operator()(int m) const { return m + (m >> 4); }
+};
+
+// ---------------------------------------------------------------------------
+// Per-step device state and integrator tables
+// ---------------------------------------------------------------------------
+struct StepDev {
+    double t, dt, t0, nu, cfl;
+    double force_target;
+    double umax;                     // last CFL speed bound (true velocity)
+    unsigned long long umax_bits;    // running max of the stage-1 z pass (bits of T, non-negative)
+    long long iters;
+    int status;                      // 0 ok; 5 numeric
+    int pad;
+};
+
+enum { INT_IFRK4 = 0, INT_RK4CN = 1 };
+// P5 modes
+enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAIN = 9 };
+
+// ---------------------------------------------------------------------------
+// P1: inverse FFT along kx with curl-on-load.
+// grid (ntile, NKY); block TT*P; smem N*TT complex.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void __launch_bounds__(tile_a<T, N>() * Plans<N>::A::P)
+k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
+    using G = Geo<N>;
+    using PL = typename Plans<N>::A;
+    constexpr int TT = tile_a<T, N>();
+    constexpr int E = PL::E, P = PL::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
+    const int t = threadIdx.x % TT, p = threadIdx.x / TT;
+    const int kz = blockIdx.x * TT + t;
+    const int ky = (int)blockIdx.y - G::KC;
+    const int j = ky < 0 ? ky + N : ky;
+    // whole CTA idle when every column of the tile is outside the circle
+    const int kz0 = blockIdx.x * TT;
+    if (ky * ky + kz0 * kz0 > G::KC2) return;
+    const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
+    const int rem = G::KC2 - ky * ky - kz * kz;
+    const long long off = (long long)j * G::NZP + kz;
+    const long long xs = (long long)N * G::NZP;
+    const T scale = T(1) / (T(N) * T(N) * T(N));
+    StridedIdx<TT> sidx{t};
+    SyncBlock sync;
+
+    auto load = [&](int c, cx<T>(&v)[E], bool ikx) {
+        const cx<T>* src = U + (long long)c * G::FS + off;
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int i = p + P * s;
+            const int kx = kof<N>(i);
+            cx<T> a = czero<T>();
+            if (colok && kx * kx <= rem) {
+                a = src[(long long)i * xs] * scale;
+                if (ikx) a = mul_i(a) * T(kx);
+            }
+            v[s] = a;
+        }
+    };
+    auto store = [&](int f, const cx<T>(&v)[E]) {
+        if (!colok) return;
+        cx<T>* dst = W + (long long)f * G::FS + off;
+#pragma unroll
+        for (int s = 0; s < E; ++s) dst[(long long)(p + P * s) * xs] = v[s];
+    };
+
+    cx<T> A[E], B[E];
+    const T fky = T(ky), fkz = T(kz);
+    // ux, kept as Tx
+    load(0, A, false);
+    PL::inv(A, sbuf, p, tw, sidx, sync);
+    store(0, A);
+    // wz = T(i kx uy) - i ky Tx
+    load(1, B, true);
+    PL::inv(B, sbuf, p, tw, sidx, sync);
+#pragma unroll
+    for (int s = 0; s < E; ++s) B[s] = B[s] - mul_i(A[s]) * fky;
+    store(5, B);
+    // wy = i kz Tx - T(i kx uz)
+    load(2, B, true);
+    PL::inv(B, sbuf, p, tw, sidx, sync);
+#pragma unroll
+    for (int s = 0; s < E; ++s) B[s] = mul_i(A[s]) * fkz - B[s];
+    store(4, B);
+    // uy, kept as Ty
+    load(1, A, false);
+    PL::inv(A, sbuf, p, tw, sidx, sync);
+    store(1, A);
+    // uz, then wx = i ky Tz - i kz Ty
+    load(2, B, false);
+    PL::inv(B, sbuf, p, tw, sidx, sync);
+    store(2, B);
+#pragma unroll
+    for (int s = 0; s < E; ++s) B[s] = mul_i(B[s]) * fky - mul_i(A[s]) * fkz;
+    store(3, B);
+}
+
+// ---------------------------------------------------------------------------
+// P2 / P4: FFT along y, in place. grid (ntile, N, nfields).
+// Inverse: inputs only where ky^2 + kz^2 <= KC^2, outputs every y.
+// Forward: inputs every y, outputs only where ky^2 + kz^2 <= KC^2.
+// ---------------------------------------------------------------------------
+template <typename T, int N, bool INV>
+__global__ void __launch_bounds__(tile_a<T, N>() * Plans<N>::A::P)
+k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
+    using G = Geo<N>;
+    using PL = typename Plans<N>::A;
+    constexpr int TT = tile_a<T, N>();
+    constexpr int E = PL::E, P = PL::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
+    const int t = threadIdx.x % TT, p = threadIdx.x / TT;
+    const int kz = blockIdx.x * TT + t;
+    const bool colok = kz <= G::KC;
+    const int rem = G::KC2 - kz * kz;
+    cx<T>* base = W + (long long)blockIdx.z * G::FS + (long long)blockIdx.y * N * G::NZP + kz;
+    StridedIdx<TT> sidx{t};
+    SyncBlock sync;
+    cx<T> v[E];
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+        const int jj = p + P * s;
+        const int ky = kof<N>(jj);
+        bool in = colok;
+        if (INV) in = in && (ky * ky <= rem);
+        v[s] = in ? base[(long long)jj * G::NZP] : czero<T>();
+    }
+    if (INV) PL::inv(v, sbuf, p, tw, sidx, sync);
+    else PL::fwd(v, sbuf, p, tw, sidx, sync);
+    if (colok) {
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int jj = p + P * s;
+            const int ky = kof<N>(jj);
+            if (INV || ky * ky <= rem) base[(long long)jj * G::NZP] = v[s];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// P3: z lines. MODE 0: c2r(6) -> u x w -> r2c(3) (fused hot path);
+// MODE 1: c2r(6) -> real out [6][N][N][N]; MODE 2: real in [3][N][N][N] -> r2c(3).
+// A CTA takes ZP line pairs; thread groups g = 0..2 each own one complex FFT.
+// c2r packs two real lines into one complex transform (fields 2g, 2g+1);
+// r2c packs (Nx_a + i Ny_a), (Nx_b + i Ny_b), (Nz_a + i Nz_b) and separates the
+// spectra with Z[m] and conj(Z[N-m]).
+// ---------------------------------------------------------------------------
+template <typename T> struct Bits;
+template <> struct Bits<float> {
+    __device__ static void amax(unsigned long long* p, float v) {
+        atomicMax(reinterpret_cast<unsigned int*>(p), __float_as_uint(v));
+    }
+};
+template <> struct Bits<double> {
+    __device__ static void amax(unsigned long long* p, double v) {
+        atomicMax(p, (unsigned long long)__double_as_longlong(v));
+    }
+};
+
+template <int N> constexpr int zpad() { return N + (N >> 4); }
+
+template <typename T, int N, int MODE>
+__global__ void __launch_bounds__(3 * Plans<N>::A::P * zpairs<N>())
+k_zpass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, T* __restrict__ real,
+        unsigned long long* __restrict__ umax_bits, int want_umax) {
+    using G = Geo<N>;
+    using PL = typename Plans<N>::A;
+    constexpr int E = PL::E, P = PL::P, ZP = zpairs<N>();
+    constexpr int XS = zpad<N>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* xbuf = reinterpret_cast<cx<T>*>(smem_raw);                       // [ZP][3][XS]
+    T* R = reinterpret_cast<T*>(smem_raw + sizeof(cx<T>) * ZP * 3 * XS);     // [ZP][2][6][N]
+    const int p = threadIdx.x % P;
+    const int g = (threadIdx.x / P) % 3;
+    const int lp = threadIdx.x / (3 * P);
+    const long long pair = (long long)blockIdx.x * ZP + lp;
+    const long long la = 2 * pair;
+    cx<T>* sb = xbuf + (lp * 3 + g) * XS;
+    T* Rl = R + (long long)lp * 12 * N;   // [2][6][N]
+    PaddedIdx sidx;
+    SyncBlock sync;
+    constexpr long long NL = (long long)N * N;   // lines
+
+    if (MODE == 0 || MODE == 1) {
+#pragma unroll 1
+        for (int L = 0; L < 2; ++L) {
+            const cx<T>* A = W + (long long)(2 * g) * G::FS + (la + L) * G::NZP;
+            const cx<T>* B = W + (long long)(2 * g + 1) * G::FS + (la + L) * G::NZP;
+            cx<T> v[E];
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                const int m = p + P * s;
+                cx<T> z = czero<T>();
+                if (m == 0) {
+                    z = mk(A[0].x, B[0].x);
+                } else if (m <= G::KC) {
+                    cx<T> a = A[m], b = B[m];
+                    z = mk(a.x - b.y, a.y + b.x);
+                } else if (m >= N - G::KC) {
+                    cx<T> a = A[N - m], b = B[N - m];
+                    z = mk(a.x + b.y, b.x - a.y);
+                }
+                v[s] = z;
+            }
+            PL::inv(v, sb, p, tw, sidx, sync);
+            T* ra = Rl + (L * 6 + 2 * g) * N;
+            T* rb = ra + N;
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                ra[p + P * s] = v[s].x;
+                rb[p + P * s] = v[s].y;
+            }
+        }
+        __syncthreads();
+        if (MODE == 1) {
+            // real out: [6][N*N lines][N]
+            for (int idx = threadIdx.x; idx < ZP * 12 * N; idx += blockDim.x) {
+                const int lpp = idx / (12 * N);
+                const int rem = idx % (12 * N);
+                const int L = rem / (6 * N);
+                const int f = (rem / N) % 6;
+                const int n = rem % N;
+                const long long line = 2 * ((long long)blockIdx.x * ZP + lpp) + L;
+                real[(long long)f * NL * N + line * N + n] = R[(long long)lpp * 12 * N + (L * 6 + f) * N + n];
+            }
+            return;
+        }
+        // u x w in place over the u slots; CFL bound on the true velocity
+        T um = T(0);
+        for (int idx = threadIdx.x; idx < ZP * 2 * N; idx += blockDim.x) {
+            const int lpp = idx / (2 * N);
+            const int L = (idx / N) % 2;
+            const int n = idx % N;
+            T* r = R + (long long)lpp * 12 * N + L * 6 * N + n;
+            const T u0 = r[0], u1 = r[N], u2 = r[2 * N];
+            const T w0 = r[3 * N], w1 = r[4 * N], w2 = r[5 * N];
+            r[0] = u1 * w2 - u2 * w1;
+            r[N] = u2 * w0 - u0 * w2;
+            r[2 * N] = u0 * w1 - u1 * w0;
+            um = fmax(um, fabs(u0) + fabs(u1) + fabs(u2));
+        }
+        if (want_umax) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) um = fmax(um, __shfl_xor_sync(0xffffffffu, um, o));
+            if ((threadIdx.x & 31) == 0) Bits<T>::amax(umax_bits, um);
+        }
+        __syncthreads();
+    } else {
+        // MODE 2: real fields in
+        for (int idx = threadIdx.x; idx < ZP * 6 * N; idx += blockDim.x) {
+            const int lpp = idx / (6 * N);
+            const int rem = idx % (6 * N);
+            const int L = rem / (3 * N);
+            const int f = (rem / N) % 3;
+            const int n = rem % N;
+            const long long line = 2 * ((long long)blockIdx.x * ZP + lpp) + L;
+            R[(long long)lpp * 12 * N + (L * 6 + f) * N + n] = real[(long long)f * NL * N + line * N + n];
+        }
+        __syncthreads();
+    }
+
+    // forward: group 0 -> line a (Nx + i Ny), 1 -> line b, 2 -> Nz_a + i Nz_b
+    {
+        const T* ra;
+        const T* rb;
+        if (g == 0) { ra = Rl; rb = Rl + N; }
+        else if (g == 1) { ra = Rl + 6 * N; rb = Rl + 7 * N; }
+        else { ra = Rl + 2 * N; rb = Rl + 8 * N; }
+        cx<T> v[E];
+#pragma unroll
+        for (int s = 0; s < E; ++s) v[s] = mk(ra[p + P * s], rb[p + P * s]);
+        PL::fwd(v, sb, p, tw, sidx, sync);
+#pragma unroll
+        for (int s = 0; s < E; ++s) sb[sidx(p + P * s)] = v[s];
+        __syncthreads();
+        cx<T>* outA;
+        cx<T>* outB;
+        if (g == 0) { outA = W + la * G::NZP; outB = W + G::FS + la * G::NZP; }
+        else if (g == 1) { outA = W + (la + 1) * G::NZP; outB = W + G::FS + (la + 1) * G::NZP; }
+        else { outA = W + 2 * G::FS + la * G::NZP; outB = W + 2 * G::FS + (la + 1) * G::NZP; }
+        const T half = T(0.5);
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int m = p + P * s;
+            if (m <= G::KC) {
+                const cx<T> zm = sb[sidx(m)];
+                const cx<T> zc = conjg(sb[sidx((N - m) % N)]);
+                const cx<T> sum = zm + zc, dif = zm - zc;
+                outA[m] = sum * half;
+                outB[m] = mk(dif.y * half, -dif.x * half);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// P5: forward FFT along x of the 3 product fields, then per mode the Leray
+// projection, dealias mask and RK stage update. grid (ntile, NKY).
+// tab[k2] holds (E_half, E_full) for IF-RK4 or (a, b) = ((2-D)/(2+D),
+// 2h/(2+D)) for RK4CN stage 4, computed in FP64 and rounded to T.
+// ---------------------------------------------------------------------------
+template <typename T, int N, int INTEG, int MODE>
+__global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
+k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
+       cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
+       const cx<T>* __restrict__ tab) {
+    using G = Geo<N>;
+    using PL = typename Plans<N>::X;
+    constexpr int TT = tile_x<T, N>();
+    constexpr int E = PL::E, P = PL::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
+    const int t = threadIdx.x % TT, p = threadIdx.x / TT;
+    const int kz = blockIdx.x * TT + t;
+    const int ky = (int)blockIdx.y - G::KC;
+    const int j = ky < 0 ? ky + N : ky;
+    const int kz0 = blockIdx.x * TT;
+    if (ky * ky + kz0 * kz0 > G::KC2) return;
+    const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
+    const long long off = (long long)j * G::NZP + kz;
+    const long long xs = (long long)N * G::NZP;
+    StridedIdx<TT> sidx{t};
+    SyncBlock sync;
+
+    cx<T> F[3][E];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const cx<T>* src = W + (long long)c * G::FS + off;
+#pragma unroll
+        for (int s = 0; s < E; ++s) F[c][s] = colok ? src[(long long)(p + P * s) * xs] : czero<T>();
+        PL::fwd(F[c], sbuf, p, tw, sidx, sync);
+    }
+    if (!colok) return;
+
+    T h = T(0);
+    if (MODE <= X_STAGE4) h = T(sd->dt);
+    const int rem = G::KC2 - ky * ky - kz * kz;
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+        const int i = p + P * s;
+        const int kx = kof<N>(i);
+        if (kx * kx > rem) continue;
+        const int k2 = kx * kx + ky * ky + kz * kz;
+        cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
+        if (MODE != X_PLAIN) {
+            if (k2 > 0) {
+                const T kinv = T(1) / T(k2);
+                const cx<T> kdn = n0 * T(kx) + n1 * T(ky) + n2 * T(kz);
+                n0 = n0 - kdn * (T(kx) * kinv);
+                n1 = n1 - kdn * (T(ky) * kinv);
+                n2 = n2 - kdn * (T(kz) * kinv);
+            } else {
+                n0 = n1 = n2 = czero<T>();
+            }
+        }
+        const long long idx = (long long)i * xs + off;
+        cx<T> nn[3] = {n0, n1, n2};
+        if (MODE == X_RHS || MODE == X_PLAIN) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ACC[c * G::FS + idx] = nn[c];
+            continue;
+        }
+        if (INTEG == INT_IFRK4) {
+            const cx<T> ef = ldg(&tab[k2]);
+            const T Eh = ef.x, Ef = ef.y;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long q = c * G::FS + idx;
+                if (MODE == X_STAGE1) {
+                    const cx<T> u = U[q];
+                    UT[q] = (u + nn[c] * (h * T(0.5))) * Eh;
+                    ACC[q] = (u + nn[c] * (h / T(6))) * Ef;
+                } else if (MODE == X_STAGE2) {
+                    const cx<T> u = U[q];
+                    UT[q] = u * Eh + nn[c] * (h * T(0.5));
+                    ACC[q] = ACC[q] + nn[c] * (h / T(3) * Eh);
+                } else if (MODE == X_STAGE3) {
+                    const cx<T> u = U[q];
+                    UT[q] = u * Ef + nn[c] * (h * Eh);
+                    ACC[q] = ACC[q] + nn[c] * (h / T(3) * Eh);
+                } else {
+                    U[q] = ACC[q] + nn[c] * (h / T(6));
+                }
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long q = c * G::FS + idx;
+                if (MODE == X_STAGE1) {
+                    UT[q] = U[q] + nn[c] * (h * T(0.5));
+                    ACC[q] = nn[c] * (T(1) / T(6));
+                } else if (MODE == X_STAGE2) {
+                    UT[q] = U[q] + nn[c] * (h * T(0.5));
+                    ACC[q] = ACC[q] + nn[c] * (T(1) / T(3));
+                } else if (MODE == X_STAGE3) {
+                    UT[q] = U[q] + nn[c] * h;
+                    ACC[q] = ACC[q] + nn[c] * (T(1) / T(3));
+                } else {
+                    const cx<T> ab = ldg(&tab[k2]);
+                    U[q] = U[q] * ab.x + (ACC[q] + nn[c] * (T(1) / T(6))) * ab.y;
+                }
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Integrator tables (FP64 exponentials), optionally after a CFL step choice.
+// tab[k2], k2 = 0..KC2. IF-RK4: (exp(-nu k2^p h/2), exp(-nu k2^p h));
+// RK4CN: ((2-D)/(2+D), 2h/(2+D)), D = h nu k2^p (solver.c:580-603).
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void k_tables(cx<T>* __restrict__ tab, StepDev* __restrict__ sd, int integ, int vp, int use_cfl) {
+    using G = Geo<N>;
+    double h = sd->dt;
+    if (use_cfl) {
+        const unsigned long long b = sd->umax_bits;
+        double um = sizeof(T) == 4 ? (double)__uint_as_float((unsigned)b) : __longlong_as_double((long long)b);
+        double hn = (um > 0.0) ? sd->cfl * (2.0 * 3.14159265358979323846 / (double)N) / um : h;
+        if (!(hn > 0.0) || !isfinite(hn)) hn = h;
+        h = hn;
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
+            sd->dt = hn;
+            sd->umax = um;
+            if (!isfinite(um)) sd->status = 5;
+        }
+    }
+    const int k2 = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k2 > G::KC2) return;
+    const double kk = (double)k2;
+    const double L = sd->nu * (vp == 2 ? kk * kk : kk);
+    cx<T> e;
+    if (integ == INT_IFRK4) {
+        e.x = T(exp(-0.5 * h * L));
+        e.y = T(exp(-h * L));
+    } else {
+        const double D = h * L;
+        e.x = T((2.0 - D) / (2.0 + D));
+        e.y = T(2.0 * h / (2.0 + D));
+    }
+    tab[k2] = e;
+}
+
+// ---------------------------------------------------------------------------
+// End of step: shell-energy forcing (new component) and time bookkeeping
+// (solver.c:193). One CTA of 256 threads; deterministic FP64 reduction.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int force_k, int use_cfl) {
+    using G = Geo<N>;
+    __shared__ double red[256];
+    const int kb = force_k;
+    const int side = 2 * kb + 1;
+    const int nbox = side * side * (kb + 1);
+    const long long k2max = (long long)kb * (kb + 1);
+    double e = 0.0;
+    if (kb > 0) {
+        for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+            const int kx = q % side - kb, ky = (q / side) % side - kb, kz = q / (side * side);
+            const long long k2 = (long long)kx * kx + ky * ky + kz * kz;
+            if (k2 == 0 || k2 > k2max || k2 > G::KC2) continue;
+            const int i = kx < 0 ? kx + N : kx, j = ky < 0 ? ky + N : ky;
+            const long long idx = ((long long)i * N + j) * G::NZP + kz;
+            const double m = (kz == 0) ? 1.0 : 2.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const cx<T> v = U[c * G::FS + idx];
+                e += m * ((double)v.x * (double)v.x + (double)v.y * (double)v.y);
+            }
+        }
+    }
+    red[threadIdx.x] = e;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    const double en = red[0] * 8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846 * 0.5 /
+                      ((double)N * N * N * (double)N * N * N);
+    if (kb > 0 && en > 0.0 && sd->force_target > 0.0) {
+        const T sc = T(sqrt(sd->force_target / en));
+        for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
+            const int kx = q % side - kb, ky = (q / side) % side - kb, kz = q / (side * side);
+            const long long k2 = (long long)kx * kx + ky * ky + kz * kz;
+            if (k2 == 0 || k2 > k2max || k2 > G::KC2) continue;
+            const int i = kx < 0 ? kx + N : kx, j = ky < 0 ? ky + N : ky;
+            const long long idx = ((long long)i * N + j) * G::NZP + kz;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) U[c * G::FS + idx] = U[c * G::FS + idx] * sc;
+        }
+    }
+    if (threadIdx.x == 0) {
+        sd->iters += 1;
+        if (use_cfl) sd->t += sd->dt;
+        else sd->t = sd->t0 + (double)sd->iters * sd->dt;
+        if (!isfinite(en)) sd->status = 5;
+        sd->umax_bits = 0ull;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Diagnostics (ComputeSystemMeasurables, solver.c:1142-1276; D4 fixed).
+// A warp walks one (kx, ky) line at a time, lanes over consecutive kz; the
+// shell index round(|k|) is non-decreasing along kz, so a segmented warp scan
+// merges equal-shell lanes and each segment's last lane adds its sum to the
+// warp's private shared-memory histogram. Per-CTA partials (5 totals +
+// 2*NSP bins) go to global memory; k_measure_reduce sums them in a fixed
+// order. Everything is FP64 and the result is bitwise reproducible.
+// ---------------------------------------------------------------------------
+constexpr int MEAS_WARPS = 8;
+template <int N> constexpr int meas_lines_per_cta() { return 64; }
+
+template <typename T, int N>
+__global__ void __launch_bounds__(MEAS_WARPS * 32)
+k_measure(const cx<T>* __restrict__ U, double nu, int vp, double* __restrict__ part) {
+    using G = Geo<N>;
+    constexpr int NSP = G::NSP;
+    constexpr int LPC = meas_lines_per_cta<N>();
+    __shared__ double hist[MEAS_WARPS][2][NSP];
+    __shared__ double tots[MEAS_WARPS][5];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    for (int q = threadIdx.x; q < MEAS_WARPS * 2 * NSP; q += blockDim.x) (&hist[0][0][0])[q] = 0.0;
+    __syncthreads();
+    double s_en = 0, s_ens = 0, s_pal = 0, s_hel = 0, s_dis = 0;
+    const long long nlines = (long long)N * G::NKY;   // (kx index, ky row) pairs
+    for (int l = w; l < LPC; l += MEAS_WARPS) {
+        const long long line = (long long)blockIdx.x * LPC + l;
+        if (line >= nlines) break;
+        const int i = (int)(line / G::NKY);
+        const int ky = (int)(line % G::NKY) - G::KC;
+        const int kx = kof<N>(i);
+        const int j = ky < 0 ? ky + N : ky;
+        const int r2 = kx * kx + ky * ky;
+        if (r2 > G::KC2) continue;
+        for (int kz0 = 0; kz0 <= G::KC; kz0 += 32) {
+            const int kz = kz0 + lane;
+            const int k2 = r2 + kz * kz;
+            const bool in = (kz <= G::KC) && (k2 <= G::KC2);
+            double eu = 0, ew = 0;
+            int bin = 0x7fffffff;
+            if (in) {
+                const long long idx = ((long long)i * N + j) * G::NZP + kz;
+                const cx<T> a0 = U[idx], a1 = U[G::FS + idx], a2 = U[2 * G::FS + idx];
+                const double ux = a0.x, uxi = a0.y, uy = a1.x, uyi = a1.y, uz = a2.x, uzi = a2.y;
+                const double fkx = kx, fky = ky, fkz = kz;
+                // w = i k x u  ->  re(w) = -(k x u_im), im(w) = k x u_re
+                const double wxr = -(fky * uzi - fkz * uyi), wxi = fky * uz - fkz * uy;
+                const double wyr = -(fkz * uxi - fkx * uzi), wyi = fkz * ux - fkx * uz;
+                const double wzr = -(fkx * uyi - fky * uxi), wzi = fkx * uy - fky * ux;
+                const double cxr = -(fky * wzi - fkz * wyi), cxi = fky * wzr - fkz * wyr;
+                const double cyr = -(fkz * wxi - fkx * wzi), cyi = fkz * wxr - fkx * wzr;
+                const double czr = -(fkx * wyi - fky * wxi), czi = fkx * wyr - fky * wxr;
+                eu = ux * ux + uxi * uxi + uy * uy + uyi * uyi + uz * uz + uzi * uzi;
+                ew = wxr * wxr + wxi * wxi + wyr * wyr + wyi * wyi + wzr * wzr + wzi * wzi;
+                const double ec = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
+                // helicity Re(u . conj(w)); the reference's Re(u . w) (solver.c:1227)
+                // is identically zero because u . (k x u) = 0 (defect D12, fixed)
+                const double hel = (ux * wxr + uxi * wxi) + (uy * wyr + uyi * wyi) + (uz * wzr + uzi * wzi);
+                const double kk = (double)k2;
+                const double pre = nu * (vp == 2 ? kk * kk : kk);
+                const double m = (kz == 0) ? 1.0 : 2.0;
+                eu *= m;
+                ew *= m;
+                s_en += eu;
+                s_ens += ew;
+                s_pal += m * ec;
+                s_hel += m * hel;
+                s_dis += pre * eu;
+                bin = (int)rint(sqrt(kk));   // k2 is never (n+1/2)^2, so rint == round
+            }
+            // segmented inclusive scan over lanes with equal bins
+            double se = eu, sw = ew;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const double te = __shfl_up_sync(0xffffffffu, se, o);
+                const double tw2 = __shfl_up_sync(0xffffffffu, sw, o);
+                const int tb = __shfl_up_sync(0xffffffffu, bin, o);
+                if (lane >= o && tb == bin) {
+                    se += te;
+                    sw += tw2;
+                }
+            }
+            const int nb = __shfl_down_sync(0xffffffffu, bin, 1);
+            if (in && (lane == 31 || nb != bin)) {
+                hist[w][0][bin] += se;
+                hist[w][1][bin] += sw;
+            }
+        }
+    }
+    // totals: fixed-order warp tree, then fixed warp order
+    double v[5] = {s_en, s_ens, s_pal, s_hel, s_dis};
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+        if (lane == 0) tots[w][q] = v[q];
+    }
+    __syncthreads();
+    double* out = part + (long long)blockIdx.x * (5 + 2 * NSP);
+    if (threadIdx.x < 5) {
+        double a = 0;
+        for (int q = 0; q < MEAS_WARPS; ++q) a += tots[q][threadIdx.x];
+        out[threadIdx.x] = a;
+    }
+    for (int b = threadIdx.x; b < 2 * NSP; b += blockDim.x) {
+        double a = 0;
+        for (int q = 0; q < MEAS_WARPS; ++q) a += hist[q][b / NSP][b % NSP];
+        out[5 + b] = a;
+    }
+}
+
+// Column sums of the partials in CTA order, then the reference scalings
+// (defined in ns3d_misc.cu).
+__global__ void k_measure_reduce(const double* __restrict__ part, int nparts, int width, int nsp,
+                                 double N3sq, double* __restrict__ out);
+
+// ---------------------------------------------------------------------------
+// Layout conversion between the reference layout (complex double
+// [N][N][N/2+1][3]) and the device layout; modes outside the sphere dropped.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void k_pack(const double2* __restrict__ ref, cx<T>* __restrict__ U) {
+    using G = Geo<N>;
+    constexpr int NF = N / 2 + 1;
+    const long long total = (long long)N * N * G::NZP;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(q % G::NZP);
+        const long long ij = q / G::NZP;
+        const int j = (int)(ij % N), i = (int)(ij / N);
+        const int kx = kof<N>(i), ky = kof<N>(j);
+        const bool in = kz <= G::KC && kx * kx + ky * ky + kz * kz <= G::KC2;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            cx<T> v = czero<T>();
+            if (in) {
+                const double2 d = ref[(ij * NF + kz) * 3 + c];
+                v = mk(T(d.x), T(d.y));
+            }
+            U[c * G::FS + q] = v;
+        }
+    }
+}
+
+template <typename T, int N>
+__global__ void k_unpack(const cx<T>* __restrict__ U, double2* __restrict__ ref) {
+    using G = Geo<N>;
+    constexpr int NF = N / 2 + 1;
+    const long long total = (long long)N * N * NF;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(q % NF);
+        const long long ij = q / NF;
+        const int j = (int)(ij % N), i = (int)(ij / N);
+        const int kx = kof<N>(i), ky = kof<N>(j);
+        const bool in = kz <= G::KC && kx * kx + ky * ky + kz * kz <= G::KC2;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double2 d = make_double2(0.0, 0.0);
+            if (in) {
+                const cx<T> v = U[c * G::FS + ij * G::NZP + kz];
+                d = make_double2((double)v.x, (double)v.y);
+            }
+            ref[q * 3 + c] = d;
+        }
+    }
+}
+
+// real [6][N][N][N] (u then w) -> reference real layout [N][N][N+2][3] x2
+template <typename T, int N>
+__global__ void k_real_unpack(const T* __restrict__ R, double* __restrict__ u, double* __restrict__ w) {
+    const long long total = (long long)N * N * (N + 2);
+    const long long M = (long long)N * N * N;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q % (N + 2));
+        const long long ij = q / (N + 2);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            double a = 0.0, b = 0.0;
+            if (k < N) {
+                a = (double)R[c * M + ij * N + k];
+                b = (double)R[(3 + c) * M + ij * N + k];
+            }
+            if (u) u[q * 3 + c] = a;
+            if (w) w[q * 3 + c] = b;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Initial conditions
+// ---------------------------------------------------------------------------
+// TAYLOR_GREEN (solver.c:1557-1568, KAPPA = 1) and SHAPIRO (solver.c:1579-1595,
+// A = 2, K = L = M = 2) in real space, real [3][N][N][N], FP64 evaluation.
+// SHAPIRO uses w = A cos(Kx) cos(Ly) sin(Mz), Shapiro's exact Beltrami
+// solution; the reference's cos(Mz) (solver.c:1593) is not divergence free.
+template <typename T, int N>
+__global__ void k_fill_real(T* __restrict__ R, int kind) {
+    const long long M = (long long)N * N * N;
+    const double dx = 2.0 * 3.14159265358979323846 / (double)N;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < M; q += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(q % N), j = (int)((q / N) % N), i = (int)(q / ((long long)N * N));
+        const double x = i * dx, y = j * dx, z = k * dx;
+        double a, b, c;
+        if (kind == 0) {
+            a = sin(x) * cos(y) * cos(z);
+            b = -cos(x) * sin(y) * cos(z);
+            c = 0.0;
+        } else {
+            const double A = 2.0, K = 2.0, L = 2.0, Mm = 2.0;
+            const double lam = sqrt(K * K + L * L + Mm * Mm);
+            a = -A / (K * K + L * L) * (lam * L * cos(K * x) * sin(L * y) * sin(Mm * z) + Mm * K * sin(K * x) * cos(L * y) * cos(Mm * z));
+            b = A / (K * K + L * L) * (lam * K * sin(K * x) * cos(L * y) * sin(Mm * z) - Mm * L * cos(K * x) * sin(L * y) * cos(Mm * z));
+            c = A * cos(K * x) * cos(L * y) * sin(Mm * z);
+        }
+        R[q] = T(a);
+        R[M + q] = T(b);
+        R[2 * M + q] = T(c);
+    }
+}
+
+// SplitMix64 (Steele, Lea & Flood 2014): finaliser of x + golden gamma.
+__device__ __forceinline__ unsigned long long splitmix64(unsigned long long x) {
+    unsigned long long z = x + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__device__ __forceinline__ double u01(unsigned long long key, unsigned long long id, int r) {
+    return (double)(splitmix64(key ^ (id * 8ull + (unsigned long long)r)) >> 11) * 0x1.0p-53;
+}
+
+// SPECTRUM: seeded random-phase solenoidal field, |u_hat(k)| = |k| exp(-k^2/k0^2)
+// (E(k) ~ k^4 exp(-2 (k/k0)^2)), Hermitian on kz = 0; the energy is scaled
+// afterwards. Random numbers are keyed by the reference-layout index of the
+// canonical mode, so the field does not depend on the device layout.
+template <typename T, int N>
+__global__ void k_spectrum_ic(cx<T>* __restrict__ U, unsigned long long key, double k0) {
+    using G = Geo<N>;
+    constexpr int NF = N / 2 + 1;
+    const long long total = (long long)N * N * G::NZP;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(q % G::NZP);
+        const long long ij = q / G::NZP;
+        const int j = (int)(ij % N), i = (int)(ij / N);
+        const int kx = kof<N>(i), ky = kof<N>(j);
+        const long long k2 = (long long)kx * kx + (long long)ky * ky + (long long)kz * kz;
+        cx<T> o[3] = {czero<T>(), czero<T>(), czero<T>()};
+        if (kz <= G::KC && k2 > 0 && k2 <= G::KC2) {
+            bool cj = false;
+            int ci = i, cjj = j;
+            if (kz == 0 && !(kx > 0 || (kx == 0 && ky > 0))) {
+                cj = true;
+                ci = (N - i) % N;
+                cjj = (N - j) % N;
+            }
+            const unsigned long long id = (unsigned long long)(((long long)ci * N + cjj) * NF + kz);
+            double vr[3], vi[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                vr[d] = 2.0 * u01(key, id, 2 * d) - 1.0;
+                vi[d] = 2.0 * u01(key, id, 2 * d + 1) - 1.0;
+            }
+            const double ckx = kof<N>(ci), cky = kof<N>(cjj), ckz = kz;
+            const double kk = (double)k2;
+            const double kvr = ckx * vr[0] + cky * vr[1] + ckz * vr[2];
+            const double kvi = ckx * vi[0] + cky * vi[1] + ckz * vi[2];
+            vr[0] -= ckx * kvr / kk; vi[0] -= ckx * kvi / kk;
+            vr[1] -= cky * kvr / kk; vi[1] -= cky * kvi / kk;
+            vr[2] -= ckz * kvr / kk; vi[2] -= ckz * kvi / kk;
+            const double vn = sqrt(vr[0] * vr[0] + vi[0] * vi[0] + vr[1] * vr[1] + vi[1] * vi[1] + vr[2] * vr[2] + vi[2] * vi[2]);
+            if (vn > 1e-300) {
+                const double amp = sqrt(kk) * exp(-kk / (k0 * k0)) / vn;
+#pragma unroll
+                for (int d = 0; d < 3; ++d) o[d] = mk(T(amp * vr[d]), T(cj ? -amp * vi[d] : amp * vi[d]));
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) U[d * G::FS + q] = o[d];
+    }
+}
+
+template <typename T, int N>
+__global__ void k_scale(cx<T>* __restrict__ U, double s) {
+    using G = Geo<N>;
+    const long long total = 3 * G::FS;
+    const T sc = T(s);
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
+        U[q] = U[q] * sc;
+}
+
+}  // namespace ns3d

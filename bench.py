@@ -1,0 +1,323 @@
+"""Benchmark of the GB300 time-stepping hot path.
+
+Workload (the configuration the headline metric is quoted on): forced
+turbulence on a 512^3 periodic grid, FP32 bulk arithmetic with FP64
+integrating factors, time accumulator and reductions; seeded random-phase
+solenoidal initial field with E(k) ~ k^4 exp(-2 (k/4)^2) at unit energy;
+nu = 1e-3; energy of shells k <= 2 held constant; CFL 0.5; integrating-factor
+RK4; 2/3-rule dealiasing. A step is one full RK4 time step (four nonlinear
+evaluations). Synthetic data: every input is generated from a seed.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0). value = grid points x steps / second summed
+over ranks (each rank runs its own replica: the solver does not shard).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt*RK4-steps/s (512^3, FP32 bulk, forced turbulence)"
+UNIT = "grid-pt*steps/s"
+WORKLOAD = dict(workload="forced turbulence 512^3, FP32 bulk + FP64 integrating factors/reductions, IF-RK4, "
+                         "2/3 dealias, shell k<=2 energy forcing, CFL 0.5, SPECTRUM IC k0=4 seed 0",
+                N=512, nu=1e-3, cfl=0.5, k0=4.0, seed=0, forcing="shell k<=2", integrator="IF-RK4",
+                precision="fp32 bulk", l2="inputs larger than L2: each state field 369 MB > 129 MB L2")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--N", type=int, default=512)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks for N independent replicas (torch.distributed)."""
+
+    def __init__(self, ws, rank, local, use_cuda):
+        self.ws, self.rank = ws, rank
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as dist
+            backend = "nccl" if use_cuda else "gloo"
+            if use_cuda:
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.dist, self.torch = dist, torch
+            self.dev = torch.device("cuda", local) if use_cuda else torch.device("cpu")
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def read_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def read_traffic(kernel: str, N: int, prec: str):
+    """Per-launch DRAM bytes of `kernel` from the committed ncu summary, or None."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        f = line.split()
+        if len(f) >= 4 and f[0] == kernel and f[1] == f"N={N}" and f[2] == prec:
+            try:
+                return float(f[3].split("=")[1])
+            except (IndexError, ValueError):
+                return None
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, gpu: int):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={gpu}", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = [r.split(",") for r in open(self.f.name).read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = max(mx, float(r[2]))
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() == "active":
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                continue
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(N: int, seed: int = 0, nthreads: int = 0):
+    """Oracle (CPU FP64 restatement) timed on a bounded sample: one nonlinear
+    evaluation (NonlinearRHSBatch) at N^3, a quarter of an RK4 step."""
+    from oracle import oracle as O
+    o = O.Oracle(N, nu=1e-3, dt=1e-3, nthreads=nthreads)
+    o.ic("SPECTRUM", seed=seed, k0=4.0, energy=1.0)
+    u = o.get_state()
+    t0 = time.perf_counter()
+    o.rhs(u)
+    t = time.perf_counter() - t0
+    return {"value": N ** 3 / (4.0 * t), "unit": UNIT, "cores": O.threads(), "kind": "port",
+            "sample": f"one NonlinearRHSBatch at {N}^3 in FP64 ({t:.1f} s) = 1/4 of an RK4 step; "
+                      f"value = N^3 / (4 t); own mixed-radix FFT"}
+
+
+def run_reference(args, ws, rank):
+    """Reference arm: the CPU restatement of the reference's path (the reference
+    itself needs FFTW-MPI/MPI/HDF5 and cannot be built), all host threads."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    O.build()
+    N = args.N
+    o = O.Oracle(N, nu=1e-3, dt=1e-3, forcing=O.FORCE_SHELL, force_k=2)
+    o.ic("SPECTRUM", seed=0, k0=4.0, energy=1.0)
+    u = o.get_state()
+    # each step is a bounded sample: one nonlinear evaluation (1/4 of an RK4 step)
+    budget = 150.0
+    t_w = time.perf_counter()
+    o.rhs(u)
+    one = time.perf_counter() - t_w
+    steps = max(1, min(args.steps, int(budget / max(one, 1e-3))))
+    ts = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        o.rhs(u)
+        ts.append(time.perf_counter() - t0)
+    t = sum(ts) / len(ts)
+    val = N ** 3 / (4.0 * t)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": 1, "ms_per_step": 4000.0 * t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(WORKLOAD, N=N),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.threads(), "kind": "port",
+                             "sample": f"{steps} x one NonlinearRHSBatch at {N}^3 (1/4 RK4 step each); "
+                                       "value = N^3/(4 t)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, ws, rank, local):
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    pkg.lib()
+    torch.cuda.set_device(local)
+    dist = Dist(ws, rank, local, True)
+    N = args.N
+    s = pkg.Solver(N, nu=1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    s.InitialConditions("SPECTRUM", seed=0, k0=4.0, energy=1.0)
+    stream = torch.cuda.ExternalStream(s.stream)
+    s.RK4Step(args.warmup)
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    s.RK4Step(args.steps)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = ev0.elapsed_time(ev1)
+    lib_ms = s.last_step_ms()
+    ms_max = dist.max(ms)
+    value = ws * N ** 3 * args.steps / (ms_max / 1e3)
+    tot, _, _ = s.ComputeSystemMeasurables()
+    t_sim, dt_sim, iters = s.get_time()
+
+    # per-kernel device times (CUDA events on the solver stream) for the roofline
+    prof = s.profile_step(reps=2)
+    peak, peak_kind = read_peaks()
+    launches = {"k_misc": 1}
+    best = max((p for p in prof if p[0] != "k_misc"), key=lambda p: p[1] * 4)
+    ach = best[2] / (best[1] / 1e3) / 1e9
+    traffic = read_traffic(best[0], N, "fp32")
+    roofline = {"bound": "hbm", "kernel": best[0], "achieved": ach, "peak": peak, "unit": "GB/s",
+                "frac": ach / peak, "peak_kind": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": best[2], "ms_per_launch": best[1],
+                "kernels": {p[0]: {"ms": p[1], "GBps": (p[2] / (p[1] / 1e3) / 1e9) if p[2] else None} for p in prof}}
+    step_bytes = sum(p[2] * 4 for p in prof)
+    survey_bytes = 198.0 * N ** 3 * 4
+    roofline["step_compulsory_GB"] = step_bytes / 1e9
+    roofline["step_survey_model_GBps"] = survey_bytes / (ms_max / args.steps / 1e3) / 1e9
+
+    # e2e: RK4Step's host-array contract through the C ABI (pinned host buffers,
+    # H2D of u_hat, one step, D2H of u_hat, every step)
+    fshape = (N, N, N // 2 + 1, 3)
+    hin = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+    hout = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+    hin[...] = s.get_state()
+    s.step_host(hin, hout)   # warm
+    ke = max(1, args.e2e_steps)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(ke):
+        s.step_host(hin, hout)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = dist.max(e0.elapsed_time(e1))
+    nbytes = int(np.prod(fshape)) * 16
+    e2e = {"value": ws * N ** 3 * ke / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": nbytes,
+           "d2h_bytes_per_step": nbytes, "steps": ke,
+           "call": "ns3d_step_host(ctx, u_hat_in, u_hat_out), reference layout complex128[N][N][N/2+1][3]"}
+    s.close()
+    del hin, hout
+
+    fp64 = None
+    if not args.no_fp64:
+        s64 = pkg.Solver(N, nu=1e-3, dt=1e-3, cfl=0.5, precision="fp64", forcing="SHELL", force_k=2, device=local)
+        s64.InitialConditions("SPECTRUM", seed=0, k0=4.0, energy=1.0)
+        s64.RK4Step(1)
+        torch.cuda.synchronize()
+        k64 = 3
+        s64.RK4Step(k64)
+        ms64 = s64.last_step_ms()
+        v64 = N ** 3 * k64 / (ms64 / 1e3)
+        fp64 = {"value": v64, "ms_per_step": ms64 / k64, "steps": k64, "fp32_over_fp64": (value / ws) / v64}
+        s64.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(N)
+    dist.close()
+    if rank != 0:
+        return
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": dict(WORKLOAD, N=N, parallelism=f"replicas x{ws}"),
+            "clocks": clocks, "e2e": e2e, "gpu_launches": s_kernels(pkg, N) * args.steps,
+            "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
+            "library_ms_per_step": lib_ms / args.steps,
+            "state_after": {"t": t_sim, "dt": dt_sim, "iters": iters, "energy": tot["energy"]}}
+    print(json.dumps(line), flush=True)
+
+
+def s_kernels(pkg, N):
+    s = pkg.Solver(16, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2)
+    k = s.kernels_per_step
+    s.close()
+    return k
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, ws, rank)
+        return
+    run_ours(args, ws, rank, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,149 @@
+/*
+ * ns3d.h — C ABI of the GB300 (sm_103a) time-stepping hot path of a 3D periodic
+ * pseudospectral Navier–Stokes solver (drop-in for the reference's
+ * Solver/src/solver.c hot path).
+ *
+ * Everything runs on one GPU with hand-written CUDA kernels; there is no CPU
+ * fallback. Plain C types only: pointers, sizes, status codes.
+ *
+ * Host array layouts are the reference's:
+ *   Fourier: complex double (re, im) [N][N][N/2+1][3]  (solver.c:644-647)
+ *   Real:    double                  [N][N][N+2][3]    (solver.c:667)
+ * The device keeps its own layout (one array per component, only the modes
+ * inside the 2/3-rule sphere) and converts at these calls.
+ *
+ * Errors: every call returns an ns3d_status instead of the reference's
+ * fprintf + exit(1) (e.g. solver.c:1394-1397, 2047-2050). A context is bound to
+ * one CUDA stream and is not thread-safe; separate contexts are independent.
+ */
+#ifndef NS3D_H
+#define NS3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    NS3D_OK = 0,
+    NS3D_ERR_INVALID = 1,      /* bad argument (size, pointer, name)            */
+    NS3D_ERR_UNSUPPORTED = 2,  /* grid size without a compiled FFT plan         */
+    NS3D_ERR_CUDA = 3,         /* CUDA runtime error                            */
+    NS3D_ERR_NOMEM = 4,        /* device allocation failed                      */
+    NS3D_ERR_NUMERIC = 5,      /* health check: NaN/Inf or non-positive dt      */
+    NS3D_ERR_TIMEOUT = 6       /* a bounded device wait gave up                 */
+} ns3d_status;
+
+typedef enum { NS3D_FP64 = 0, NS3D_FP32 = 1 } ns3d_precision;
+typedef enum { NS3D_IFRK4 = 0, NS3D_RK4CN = 1 } ns3d_integrator;
+typedef enum { NS3D_FORCE_NONE = 0, NS3D_FORCE_SHELL = 1 } ns3d_forcing;
+
+/* Parameters: the hot-path fields of system_vars_struct (data_types.h:147-185)
+ * plus the switches that replace the reference's compile-time macros. */
+typedef struct {
+    int    N;           /* grid points per axis (cubic box, sys_vars->N)               */
+    double nu;          /* viscosity (sys_vars->NU, utils.c:150-156)                    */
+    double dt;          /* time step (sys_vars->dt); initial step when cfl > 0          */
+    double t0;          /* start time (sys_vars->t0)                                    */
+    int    visc_pow;    /* 1: nu k^2; 2: nu k^4 (HYPER_VISC, VIS_POW, data_types.h:68-71) */
+    int    integrator;  /* ns3d_integrator; RK4CN is the reference's RK4Step          */
+    int    precision;   /* ns3d_precision: FP64, or FP32 bulk with FP64 integrating
+                           factors, time accumulator and reductions                   */
+    double cfl;         /* > 0: dt = cfl * dx / max(|u|+|v|+|w|) every step (CFL_CONST)  */
+    int    forcing;     /* ns3d_forcing: SHELL holds the energy of shells
+                           1 <= round(|k|) <= force_k at its initial value            */
+    int    force_k;     /* forcing shell radius (sys_vars->force_k)                     */
+    int    device;      /* CUDA device ordinal                                          */
+    void*  stream;      /* cudaStream_t to run on, or NULL for a private stream         */
+} ns3d_params;
+
+/* Totals of ComputeSystemMeasurables (solver.c:1142-1276), with the reference's
+ * normalisation 8 pi^3 * 0.5 / N^6 and the kz-plane multiplicities. */
+typedef struct {
+    double energy;        /* tot_energy                                  */
+    double enstrophy;     /* tot_enstr                                   */
+    double palinstrophy;  /* tot_palin                                   */
+    double helicity;      /* tot_heli as Re sum u.conj(w) (see D12)      */
+    double dissipation;   /* enrg_diss                                   */
+} ns3d_measures;
+
+typedef struct ns3d_ctx ns3d_ctx;
+
+const char* ns3d_status_string(ns3d_status s);
+/* 1 when a compiled FFT plan exists for grid size N, else 0. */
+int ns3d_supported_size(int N);
+/* Length of the spectrum arrays, sys_vars->n_spect (solver.c:1384). */
+int ns3d_n_spect(int N);
+
+/* AllocateMemory + InitializeFFTWPlans + InitializeSpaceVariables
+ * (solver.c:1832-2073, 1764-1826): device state, twiddle tables, step graph. */
+ns3d_status ns3d_create(const ns3d_params* params, ns3d_ctx** out);
+/* FreeMemory (solver.c:2078-2157). */
+ns3d_status ns3d_destroy(ns3d_ctx* ctx);
+/* Message of the last failure on this context ("" when none). */
+const char* ns3d_last_error(const ns3d_ctx* ctx);
+
+/* InitialConditions (solver.c:1537-1648). Names: "TAYLOR_GREEN", "SHAPIRO",
+ * "TESTING" (zero field), "RANDOM" (the reference's srand(123456789) modes),
+ * "SPECTRUM" (new: seeded random-phase solenoidal field with
+ * E(k) ~ k^4 exp(-2 (k/k0)^2), scaled so that 0.5 <|u|^2> = energy).
+ * Other names fall back to RANDOM like the reference. Resets t, dt, iters. */
+ns3d_status ns3d_initial_condition(ns3d_ctx* ctx, const char* name, uint64_t seed,
+                                   double k0, double energy);
+
+/* Copy the state u_hat in or out (reference Fourier layout, FP64 host array).
+ * Modes outside the 2/3-rule sphere are dropped on the way in, as
+ * ApplyDealiasing does (solver.c:1630). */
+ns3d_status ns3d_set_state_host(ns3d_ctx* ctx, const double* u_hat);
+ns3d_status ns3d_get_state_host(ns3d_ctx* ctx, double* u_hat);
+
+/* RK4Step (solver.c:505-608) or IF-RK4, nsteps times on the device state,
+ * including forcing and the CFL step choice when enabled. */
+ns3d_status ns3d_step(ns3d_ctx* ctx, int nsteps);
+/* One step through host buffers: u_hat_in -> step -> u_hat_out (either may be
+ * NULL to keep the device state). This is RK4Step's host-array contract. */
+ns3d_status ns3d_step_host(ns3d_ctx* ctx, const double* u_hat_in, double* u_hat_out);
+
+/* NonlinearRHSBatch (solver.c:620-731): out = P[FFT(u x w)] / N^6, dealiased,
+ * for the dealiased part of in. Host arrays in the reference Fourier layout. */
+ns3d_status ns3d_rhs_host(ns3d_ctx* ctx, const double* u_hat_in, double* rhs_out);
+
+/* ApplyDealiasing (solver.c:1709-1756) of a host array with array_dim
+ * interleaved components (2/3 rule, defect D2 fixed). */
+ns3d_status ns3d_dealias_host(int N, double* array, int array_dim);
+
+/* ComputeSystemMeasurables (solver.c:1142-1276), defect D4 fixed. Ek and Ok
+ * (n_spect doubles each) may be NULL. Deterministic FP64 reductions. */
+ns3d_status ns3d_measurables(ns3d_ctx* ctx, ns3d_measures* out, double* Ek, double* Ok);
+
+/* Real-space velocity and vorticity normalised by 1/N^3 (hdf5_funcs.c:586-600,
+ * 662-676), reference real layout; either pointer may be NULL. */
+ns3d_status ns3d_real_space_host(ns3d_ctx* ctx, double* u, double* w);
+
+/* Time bookkeeping (solver.c:1314-1363): current t, dt and completed steps. */
+ns3d_status ns3d_get_time(ns3d_ctx* ctx, double* t, double* dt, long* iters);
+ns3d_status ns3d_set_time(ns3d_ctx* ctx, double t, double dt, long iters);
+/* Forcing target energy (set by initial conditions / set_state). */
+ns3d_status ns3d_get_forcing_target(ns3d_ctx* ctx, double* e);
+ns3d_status ns3d_set_forcing_target(ns3d_ctx* ctx, double e);
+
+/* Largest |u|+|v|+|w| over the grid for the current state (CFL numerator). */
+ns3d_status ns3d_max_speed_sum(ns3d_ctx* ctx, double* umax);
+
+/* Instrumentation for benchmarks: the stream the context runs on, the number
+ * of kernels one step launches, and the device time of the last ns3d_step
+ * call (CUDA events on the context stream), in milliseconds. */
+void* ns3d_stream(ns3d_ctx* ctx);
+int ns3d_kernels_per_step(ns3d_ctx* ctx);
+ns3d_status ns3d_last_step_ms(ns3d_ctx* ctx, float* ms);
+/* Device time of each kernel class of one step, for roofline accounting:
+ * names[i] / ms[i] for i < *count (max_count entries at most). */
+ns3d_status ns3d_profile_step(ns3d_ctx* ctx, int reps, const char** names, float* ms,
+                              double* bytes, int max_count, int* count);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

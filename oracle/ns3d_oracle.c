@@ -1,0 +1,773 @@
+/*
+ * ns3d_oracle.c — ORACLE: test infrastructure only, never product code.
+ *
+ * CPU FP64 restatement of the reference solver's time-stepping hot path
+ * (Solver/src/solver.c). Used by tests/ as the parity checker and by bench.py
+ * as the timed CPU baseline. Each function cites the reference lines it
+ * restates. The reference itself cannot be compiled here: it needs FFTW3-MPI,
+ * MPI and parallel HDF5, none of which exist on either machine.
+ *
+ * Parity pinning: the reference ships no golden vectors. This restatement is
+ * pinned by (1) its FFT against numpy.fft (pocketfft) and a direct DFT, the
+ * stand-in for the reference's FFTW calls (solver.c:656,658,683,1573,1599);
+ * (2) the reference's own known-answer test, the Shapiro exact solution
+ * (solver.c:1654-1702), and the Taylor–Green invariants E = pi^3,
+ * Omega = 3 pi^3 at t = 0; (3) an independent numpy restatement of the RHS
+ * and both integrators (tests/golden/make_golden.py).
+ *
+ * Defects of the reference (solver.c) are fixed here, each behind a flag where
+ * reproducing it is meaningful:
+ *   D1 transform logical size {N,N,N/2+1} (solver.c:55,2067): fixed, {N,N,N}.
+ *   D2 dealias keep-branch aliasing (solver.c:1741): fixed; bugcompat_dealias.
+ *   D3 TAYLOR_GREEN overwritten by random modes (solver.c:1553-1606): fixed.
+ *   D4 2.0*|x|+|y|+|z| precedence (solver.c:1232-1235): fixed; bugcompat_measures.
+ *   D12 helicity Re(u.w) without conjugation (solver.c:1227) is identically
+ *       zero: fixed to Re(u.conj(w)); bugcompat_measures keeps the old form.
+ *   D13 SHAPIRO w = A cos cos cos(Mz) (solver.c:1593, 1686) is not divergence
+ *       free: fixed to sin(Mz); bugcompat_measures keeps the old form.
+ *
+ * c2r semantics (FFTW's, restated): the two complex axes are inverted as full
+ * complex transforms, then each z line is extended by Hermitian symmetry and
+ * the imaginary parts of its kz = 0 and kz = N/2 entries are ignored.
+ */
+#include "ns3d_oracle.h"
+
+#include <complex.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+typedef double complex cplx;
+
+/* ------------------------------------------------------------------------ */
+/* Twiddles: e^{-2 pi i m / n}, reduced by quarter turns so that the         */
+/* symmetric values (1, -i, -1, i, ...) come out exact.                       */
+/* ------------------------------------------------------------------------ */
+static cplx twiddle(long m, long n) {
+    m %= n;
+    if (m < 0) m += n;
+    long q = (4 * m) / n;          /* quarter turns */
+    long r = 4 * m - q * n;        /* remainder, angle = (pi/2) * r / n */
+    const long double half_pi = acosl(-1.0L) / 2.0L;
+    long double cs, sn;
+    if (2 * r <= n) {
+        long double phi = half_pi * (long double)r / (long double)n;
+        cs = cosl(phi);
+        sn = sinl(phi);
+    } else {
+        long double phi = half_pi * (long double)(n - r) / (long double)n;
+        cs = sinl(phi);
+        sn = cosl(phi);
+    }
+    double c = (double)cs, s = (double)sn;   /* cos(theta), sin(theta) in the quadrant */
+    double cr, sr;
+    switch (q) {
+        case 0: cr = c;  sr = s;  break;
+        case 1: cr = -s; sr = c;  break;
+        case 2: cr = -c; sr = -s; break;
+        default: cr = s; sr = -c; break;
+    }
+    return cr - I * sr;            /* e^{-i theta} */
+}
+
+/* ------------------------------------------------------------------------ */
+/* Mixed-radix recursive decimation-in-time FFT (radix 4, 2, 3, 5, generic). */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int n;
+    int nfac;
+    int fac[64];
+    cplx* tw;   /* tw[m] = e^{-2 pi i m / n} */
+} fft_plan;
+
+static void plan_init(fft_plan* p, int n) {
+    p->n = n;
+    p->nfac = 0;
+    int m = n;
+    while (m % 4 == 0) { p->fac[p->nfac++] = 4; m /= 4; }
+    while (m % 2 == 0) { p->fac[p->nfac++] = 2; m /= 2; }
+    for (int f = 3; f * f <= m; f += 2)
+        while (m % f == 0) { p->fac[p->nfac++] = f; m /= f; }
+    if (m > 1) p->fac[p->nfac++] = m;
+    p->tw = (cplx*)malloc(sizeof(cplx) * (size_t)n);
+    for (int i = 0; i < n; ++i) p->tw[i] = twiddle(i, n);
+}
+
+static void plan_free(fft_plan* p) { free(p->tw); p->tw = NULL; }
+
+/* out[k] = sum_j in[j*is] * w^{jk}, w = e^{-+2 pi i/n}; twiddle index scale ts */
+static void fft_rec(const cplx* in, long is, cplx* out, int n, const int* fac,
+                    const cplx* tw, int ts, int inv) {
+    if (n == 1) { out[0] = in[0]; return; }
+    const int R = fac[0], m = n / R;
+    for (int r = 0; r < R; ++r) fft_rec(in + r * is, is * R, out + r * m, m, fac + 1, tw, ts * R, inv);
+    const int N = n * ts;   /* size of the twiddle table */
+#define TW(e) (inv ? conj(tw[(long)(e) * ts % N]) : tw[(long)(e) * ts % N])
+    if (R == 2) {
+        for (int k = 0; k < m; ++k) {
+            cplx a = out[k], b = out[m + k] * TW(k);
+            out[k] = a + b;
+            out[m + k] = a - b;
+        }
+    } else if (R == 4) {
+        const cplx mi = inv ? I : -I;   /* w^{n/4} */
+        for (int k = 0; k < m; ++k) {
+            cplx a0 = out[k];
+            cplx a1 = out[m + k] * TW(k);
+            cplx a2 = out[2 * m + k] * TW(2 * k);
+            cplx a3 = out[3 * m + k] * TW(3 * k);
+            cplx s02 = a0 + a2, d02 = a0 - a2, s13 = a1 + a3, d13 = (a1 - a3) * mi;
+            out[k] = s02 + s13;
+            out[m + k] = d02 + d13;
+            out[2 * m + k] = s02 - s13;
+            out[3 * m + k] = d02 - d13;
+        }
+    } else {
+        cplx a[64];
+        cplx wr[64];
+        for (int q = 0; q < R; ++q) wr[q] = inv ? conj(twiddle(q, R)) : twiddle(q, R);
+        for (int k = 0; k < m; ++k) {
+            for (int r = 0; r < R; ++r) a[r] = out[r * m + k] * TW((long)r * k);
+            for (int q = 0; q < R; ++q) {
+                cplx s = 0;
+                for (int r = 0; r < R; ++r) s += a[r] * wr[(r * q) % R];
+                out[q * m + k] = s;
+            }
+        }
+    }
+#undef TW
+}
+
+static void fft_exec(const fft_plan* p, const cplx* in, cplx* out, int inv) {
+    fft_rec(in, 1, out, p->n, p->fac, p->tw, 1, inv);
+}
+
+void orc_fft1d(int n, const double* in, double* out, int inverse) {
+    fft_plan p;
+    plan_init(&p, n);
+    fft_exec(&p, (const cplx*)in, (cplx*)out, inverse);
+    plan_free(&p);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Context                                                                   */
+/* ------------------------------------------------------------------------ */
+struct orc_ctx {
+    orc_params p;
+    int N, NF;               /* NF = N/2+1 */
+    long nF, nR;             /* complex / real element counts per component */
+    int* kx; int* ky; int* kz;
+    double* x;               /* collocation points (solver.c:1786-1823) */
+    fft_plan plan;
+    cplx* u_hat;             /* state, reference layout */
+    cplx *rk1, *rk2, *rk3, *rk4, *rk_tmp, *w_hat;
+    double *vel, *vort, *curl;
+    double t, dt;
+    long iters;
+    double force_target;
+    double last_umax;        /* max(|u|+|v|+|w|) seen by the last stage-1 RHS */
+};
+
+int orc_threads(void) {
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+int orc_n_spect(int N) {
+    /* solver.c:1384 (cubic) */
+    return (int)sqrt(3.0 * pow((double)N / 2.0, 2.0)) + 1;
+}
+
+/* InitializeSpaceVariables, solver.c:1764-1826 (single process: local_Nx = N) */
+static void init_space(orc_ctx* c) {
+    const int N = c->N;
+    for (int i = 0; i < N; ++i) {
+        c->kx[i] = (i <= N / 2) ? i : i - N;
+        c->ky[i] = (i < N / 2 + 1) ? i : -N + i;
+        c->x[i] = (double)i * (2.0 * M_PI / (double)N);
+    }
+    for (int i = 0; i < c->NF; ++i) c->kz[i] = i;
+}
+
+orc_ctx* orc_create(const orc_params* p) {
+    if (!p || p->N < 4 || (p->N % 2)) return NULL;
+    orc_ctx* c = (orc_ctx*)calloc(1, sizeof(orc_ctx));
+    c->p = *p;
+    if (c->p.visc_pow < 1) c->p.visc_pow = 1;
+#ifdef _OPENMP
+    if (p->nthreads > 0) omp_set_num_threads(p->nthreads);
+#endif
+    c->N = p->N;
+    c->NF = p->N / 2 + 1;
+    c->nF = (long)c->N * c->N * c->NF;
+    c->nR = (long)c->N * c->N * (c->N + 2);
+    c->kx = (int*)malloc(sizeof(int) * c->N);
+    c->ky = (int*)malloc(sizeof(int) * c->N);
+    c->kz = (int*)malloc(sizeof(int) * c->NF);
+    c->x = (double*)malloc(sizeof(double) * c->N);
+    init_space(c);
+    plan_init(&c->plan, c->N);
+    size_t fb = sizeof(cplx) * 3 * (size_t)c->nF, rb = sizeof(double) * 3 * (size_t)c->nR;
+    c->u_hat = (cplx*)calloc(1, fb);
+    c->rk1 = (cplx*)calloc(1, fb);
+    c->rk2 = (cplx*)calloc(1, fb);
+    c->rk3 = (cplx*)calloc(1, fb);
+    c->rk4 = (cplx*)calloc(1, fb);
+    c->rk_tmp = (cplx*)calloc(1, fb);
+    c->w_hat = (cplx*)calloc(1, fb);
+    c->vel = (double*)calloc(1, rb);
+    c->vort = (double*)calloc(1, rb);
+    c->curl = (double*)calloc(1, rb);
+    c->t = p->t0;
+    c->dt = p->dt;
+    c->iters = 0;
+    return c;
+}
+
+void orc_destroy(orc_ctx* c) {
+    if (!c) return;
+    free(c->kx); free(c->ky); free(c->kz); free(c->x);
+    plan_free(&c->plan);
+    free(c->u_hat); free(c->rk1); free(c->rk2); free(c->rk3); free(c->rk4);
+    free(c->rk_tmp); free(c->w_hat); free(c->vel); free(c->vort); free(c->curl);
+    free(c);
+}
+
+static double energy_shells(orc_ctx* c, const cplx* u, int kmax_bin);
+
+void orc_set_state(orc_ctx* c, const double* u_hat) {
+    memcpy(c->u_hat, u_hat, sizeof(cplx) * 3 * (size_t)c->nF);
+    if (c->p.forcing == ORC_FORCE_SHELL) c->force_target = energy_shells(c, c->u_hat, c->p.force_k);
+}
+void orc_get_state(const orc_ctx* c, double* u_hat) {
+    memcpy(u_hat, c->u_hat, sizeof(cplx) * 3 * (size_t)c->nF);
+}
+void orc_set_time(orc_ctx* c, double t, double dt, long iters) { c->t = t; c->dt = dt; c->iters = iters; }
+void orc_get_time(const orc_ctx* c, double* t, double* dt, long* iters) {
+    if (t) *t = c->t;
+    if (dt) *dt = c->dt;
+    if (iters) *iters = c->iters;
+}
+double orc_forcing_target(const orc_ctx* c) { return c->force_target; }
+void orc_set_forcing_target(orc_ctx* c, double e) { c->force_target = e; }
+
+/* ------------------------------------------------------------------------ */
+/* 3D transforms, batched over 3 interleaved components (replaces the FFTW   */
+/* plans of solver.c:2045-2068 with the logical size {N,N,N}, i.e. D1 fixed) */
+/* ------------------------------------------------------------------------ */
+void orc_fft_r2c(orc_ctx* c, const double* real, double* u_hat_d) {
+    const int N = c->N, NF = c->NF;
+    cplx* out = (cplx*)u_hat_d;
+    /* z: real lines -> half spectrum */
+#pragma omp parallel
+    {
+        cplx* a = (cplx*)malloc(sizeof(cplx) * N);
+        cplx* b = (cplx*)malloc(sizeof(cplx) * N);
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int d = 0; d < 3; ++d) {
+                    const double* line = real + 3 * ((long)(i * N + j) * (N + 2));
+                    for (int k = 0; k < N; ++k) a[k] = line[3 * k + d];
+                    fft_exec(&c->plan, a, b, 0);
+                    for (int k = 0; k < NF; ++k) out[3 * ((long)(i * N + j) * NF + k) + d] = b[k];
+                }
+        /* y */
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int k = 0; k < NF; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    for (int j = 0; j < N; ++j) a[j] = out[3 * ((long)(i * N + j) * NF + k) + d];
+                    fft_exec(&c->plan, a, b, 0);
+                    for (int j = 0; j < N; ++j) out[3 * ((long)(i * N + j) * NF + k) + d] = b[j];
+                }
+        /* x */
+#pragma omp for collapse(2) schedule(static)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    for (int i = 0; i < N; ++i) a[i] = out[3 * ((long)(i * N + j) * NF + k) + d];
+                    fft_exec(&c->plan, a, b, 0);
+                    for (int i = 0; i < N; ++i) out[3 * ((long)(i * N + j) * NF + k) + d] = b[i];
+                }
+        free(a);
+        free(b);
+    }
+}
+
+void orc_fft_c2r(orc_ctx* c, const double* u_hat_d, double* real) {
+    const int N = c->N, NF = c->NF;
+    const cplx* in = (const cplx*)u_hat_d;
+    cplx* tmp = (cplx*)malloc(sizeof(cplx) * 3 * (size_t)c->nF);   /* preserve input */
+#pragma omp parallel
+    {
+        cplx* a = (cplx*)malloc(sizeof(cplx) * N);
+        cplx* b = (cplx*)malloc(sizeof(cplx) * N);
+        /* x */
+#pragma omp for collapse(2) schedule(static)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    for (int i = 0; i < N; ++i) a[i] = in[3 * ((long)(i * N + j) * NF + k) + d];
+                    fft_exec(&c->plan, a, b, 1);
+                    for (int i = 0; i < N; ++i) tmp[3 * ((long)(i * N + j) * NF + k) + d] = b[i];
+                }
+        /* y */
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int k = 0; k < NF; ++k)
+                for (int d = 0; d < 3; ++d) {
+                    for (int j = 0; j < N; ++j) a[j] = tmp[3 * ((long)(i * N + j) * NF + k) + d];
+                    fft_exec(&c->plan, a, b, 1);
+                    for (int j = 0; j < N; ++j) tmp[3 * ((long)(i * N + j) * NF + k) + d] = b[j];
+                }
+        /* z: Hermitian extension, imaginary parts of kz = 0 and kz = N/2 ignored */
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int d = 0; d < 3; ++d) {
+                    const cplx* h = tmp + 3 * ((long)(i * N + j) * NF);
+                    a[0] = creal(h[d]);
+                    for (int k = 1; k < N / 2; ++k) {
+                        a[k] = h[3 * k + d];
+                        a[N - k] = conj(h[3 * k + d]);
+                    }
+                    a[N / 2] = creal(h[3 * (N / 2) + d]);
+                    fft_exec(&c->plan, a, b, 1);
+                    double* line = real + 3 * ((long)(i * N + j) * (N + 2));
+                    for (int k = 0; k < N; ++k) line[3 * k + d] = creal(b[k]);
+                    line[3 * N + d] = 0.0;
+                    line[3 * (N + 1) + d] = 0.0;
+                }
+        free(a);
+        free(b);
+    }
+    free(tmp);
+}
+
+/* ------------------------------------------------------------------------ */
+/* ApplyDealiasing, solver.c:1709-1756 (2/3 rule, __DEALIAS_23)              */
+/* ------------------------------------------------------------------------ */
+void orc_dealias(orc_ctx* c, double* arr_d, int array_dim) {
+    const int N = c->N, NF = c->NF;
+    cplx* array = (cplx*)arr_d;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long indx = (long)(i * N + j) * NF + k;
+                if (sqrt((double)c->kx[i] * c->kx[i] + c->ky[j] * c->ky[j] + c->kz[k] * c->kz[k]) > N / 3) {
+                    for (int l = 0; l < array_dim; ++l) array[array_dim * indx + l] = 0.0;
+                } else if (c->p.bugcompat_dealias) {
+                    /* D2 reproduced: solver.c:1741 copies array[indx+l] */
+                    for (int l = 0; l < array_dim; ++l) array[array_dim * indx + l] = array[indx + l];
+                }
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* NonlinearRHSBatch, solver.c:620-731                                       */
+/* ------------------------------------------------------------------------ */
+static void rhs_impl(orc_ctx* c, const cplx* u_hat, cplx* dw, int want_umax) {
+    const int N = c->N, NF = c->NF;
+    const double norm = 1.0 / pow((double)N * N * N, 2.0);
+    /* curl in Fourier space (solver.c:637-650) */
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long indx = (long)(i * N + j) * NF + k;
+                const cplx* u = u_hat + 3 * indx;
+                dw[3 * indx + 0] = I * (c->ky[j] * u[2] - c->kz[k] * u[1]);
+                dw[3 * indx + 1] = I * (c->kz[k] * u[0] - c->kx[i] * u[2]);
+                dw[3 * indx + 2] = I * (c->kx[i] * u[1] - c->ky[j] * u[0]);
+            }
+    /* to real space (solver.c:656-658) */
+    orc_fft_c2r(c, (const double*)dw, c->vort);
+    orc_fft_c2r(c, (const double*)u_hat, c->vel);
+    /* u x w (solver.c:664-677), plus the CFL speed bound on the true velocity */
+    const double inv3 = 1.0 / ((double)N * N * N);
+    double umax = 0.0;
+#pragma omp parallel for collapse(2) schedule(static) reduction(max : umax)
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < N; ++k) {
+                long indx = (long)(i * N + j) * (N + 2) + k;
+                const double* u = c->vel + 3 * indx;
+                const double* w = c->vort + 3 * indx;
+                double* o = c->curl + 3 * indx;
+                o[0] = u[1] * w[2] - u[2] * w[1];
+                o[1] = u[2] * w[0] - u[0] * w[2];
+                o[2] = u[0] * w[1] - u[1] * w[0];
+                if (want_umax) {
+                    double s = (fabs(u[0]) + fabs(u[1]) + fabs(u[2])) * inv3;
+                    if (s > umax) umax = s;
+                }
+            }
+    if (want_umax) c->last_umax = umax;
+    /* back to Fourier space (solver.c:683) */
+    orc_fft_r2c(c, c->curl, (double*)dw);
+    /* normalise + Leray projection (solver.c:689-721) */
+#pragma omp parallel for collapse(2) schedule(static)
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long indx = (long)(i * N + j) * NF + k;
+                cplx* n = dw + 3 * indx;
+                n[0] *= norm;
+                n[1] *= norm;
+                n[2] *= norm;
+                if (c->kx[i] != 0 || c->ky[j] != 0 || c->kz[k] != 0) {
+                    double kinv = 1.0 / (double)(c->kx[i] * c->kx[i] + c->ky[j] * c->ky[j] + c->kz[k] * c->kz[k]);
+                    cplx kdn = c->kx[i] * n[0] + c->ky[j] * n[1] + c->kz[k] * n[2];
+                    n[0] -= c->kx[i] * kinv * kdn;
+                    n[1] -= c->ky[j] * kinv * kdn;
+                    n[2] -= c->kz[k] * kinv * kdn;
+                } else {
+                    n[0] = n[1] = n[2] = 0.0;
+                }
+            }
+    /* dealias (solver.c:727) */
+    orc_dealias(c, (double*)dw, 3);
+}
+
+void orc_rhs(orc_ctx* c, const double* u_hat, double* rhs) {
+    rhs_impl(c, (const cplx*)u_hat, (cplx*)rhs, 0);
+}
+
+double orc_max_speed_sum(orc_ctx* c) {
+    rhs_impl(c, c->u_hat, c->rk1, 1);
+    return c->last_umax;
+}
+
+/* |k|^2 and the viscous operator nu (k^2)^p (solver.c:580-587) */
+static inline double visc(const orc_ctx* c, int i, int j, int k) {
+    double k2 = (double)(c->kx[i] * c->kx[i] + c->ky[j] * c->ky[j] + c->kz[k] * c->kz[k]);
+    return c->p.visc_pow == 2 ? c->p.nu * k2 * k2 : c->p.nu * k2;
+}
+
+/* energy in the shells 1 <= round(|k|) <= kb (forcing, new component) */
+static double energy_shells(orc_ctx* c, const cplx* u, int kb) {
+    const int N = c->N, NF = c->NF;
+    const long k2max = (long)kb * (kb + 1);   /* round(sqrt(k2)) <= kb  <=>  k2 <= kb(kb+1) */
+    double e = 0.0;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long k2 = (long)c->kx[i] * c->kx[i] + (long)c->ky[j] * c->ky[j] + (long)c->kz[k] * c->kz[k];
+                if (k2 == 0 || k2 > k2max) continue;
+                long indx = (long)(i * N + j) * NF + k;
+                double m = (k == 0 || k == NF - 1) ? 1.0 : 2.0;
+                const cplx* v = u + 3 * indx;
+                e += m * (creal(v[0] * conj(v[0])) + creal(v[1] * conj(v[1])) + creal(v[2] * conj(v[2])));
+            }
+    return 8.0 * pow(M_PI, 3.0) * 0.5 / pow((double)N * N * N, 2.0) * e;
+}
+
+static void apply_forcing(orc_ctx* c) {
+    const int N = c->N, NF = c->NF, kb = c->p.force_k;
+    const long k2max = (long)kb * (kb + 1);
+    double e = energy_shells(c, c->u_hat, kb);
+    if (!(e > 0.0) || !(c->force_target > 0.0)) return;
+    double s = sqrt(c->force_target / e);
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long k2 = (long)c->kx[i] * c->kx[i] + (long)c->ky[j] * c->ky[j] + (long)c->kz[k] * c->kz[k];
+                if (k2 == 0 || k2 > k2max) continue;
+                long indx = (long)(i * N + j) * NF + k;
+                for (int d = 0; d < 3; ++d) c->u_hat[3 * indx + d] *= s;
+            }
+}
+
+/* ------------------------------------------------------------------------ */
+/* One time step. RK4 + Crank–Nicolson factor restates RK4Step              */
+/* (solver.c:505-608). IF-RK4 is Lawson's integrating-factor RK4 (1967):     */
+/*   E = exp(-nu k^2p h/2);  k1 = N(u); k2 = N(E(u + h/2 k1));               */
+/*   k3 = N(E u + h/2 k2);  k4 = N(E^2 u + h E k3);                          */
+/*   u+ = E^2 u + h/6 (E^2 k1 + 2E (k2 + k3) + k4)                           */
+/* ------------------------------------------------------------------------ */
+#define FOR_MODES                                                   \
+    _Pragma("omp parallel for collapse(2) schedule(static)")        \
+    for (int i = 0; i < N; ++i)                                     \
+        for (int j = 0; j < N; ++j)                                 \
+            for (int k = 0; k < NF; ++k)
+
+static void one_step(orc_ctx* c) {
+    const int N = c->N, NF = c->NF;
+    cplx* u = c->u_hat;
+    const int cfl = c->p.cfl > 0.0;
+    rhs_impl(c, u, c->rk1, cfl);
+    if (cfl) {
+        if (c->last_umax > 0.0) c->dt = c->p.cfl * (2.0 * M_PI / (double)N) / c->last_umax;
+    }
+    const double h = c->dt;
+    if (c->p.integrator == ORC_RK4CN) {
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk1[x + d];
+        }
+        rhs_impl(c, c->rk_tmp, c->rk2, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk2[x + d];
+        }
+        rhs_impl(c, c->rk_tmp, c->rk3, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 1.0 * c->rk3[x + d];
+        }
+        rhs_impl(c, c->rk_tmp, c->rk4, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            double D = h * visc(c, i, j, k);
+            for (int d = 0; d < 3; ++d)
+                u[x + d] = u[x + d] * ((2.0 - D) / (2.0 + D)) +
+                           (2.0 * h / (2.0 + D)) * (1.0 / 6.0 * c->rk1[x + d] + 1.0 / 3.0 * c->rk2[x + d] +
+                                                    1.0 / 3.0 * c->rk3[x + d] + 1.0 / 6.0 * c->rk4[x + d]);
+        }
+    } else {
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            double E = exp(-0.5 * h * visc(c, i, j, k));
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * (u[x + d] + 0.5 * h * c->rk1[x + d]);
+        }
+        rhs_impl(c, c->rk_tmp, c->rk2, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            double E = exp(-0.5 * h * visc(c, i, j, k));
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * u[x + d] + 0.5 * h * c->rk2[x + d];
+        }
+        rhs_impl(c, c->rk_tmp, c->rk3, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            double E = exp(-0.5 * h * visc(c, i, j, k));
+            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * E * u[x + d] + h * E * c->rk3[x + d];
+        }
+        rhs_impl(c, c->rk_tmp, c->rk4, 0);
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            double E = exp(-0.5 * h * visc(c, i, j, k));
+            double E2 = E * E;
+            for (int d = 0; d < 3; ++d)
+                u[x + d] = E2 * u[x + d] +
+                           h / 6.0 * (E2 * c->rk1[x + d] + 2.0 * E * (c->rk2[x + d] + c->rk3[x + d]) + c->rk4[x + d]);
+        }
+    }
+    if (c->p.forcing == ORC_FORCE_SHELL) apply_forcing(c);
+    c->iters += 1;
+    if (cfl) c->t += h;
+    else c->t = c->p.t0 + (double)c->iters * h;
+}
+
+void orc_step(orc_ctx* c, int nsteps) {
+    for (int s = 0; s < nsteps; ++s) one_step(c);
+}
+
+/* ------------------------------------------------------------------------ */
+/* ComputeSystemMeasurables, solver.c:1142-1276 (D4 fixed unless bugcompat)  */
+/* totals: [energy, enstrophy, palinstrophy, helicity, energy dissipation]   */
+/* ------------------------------------------------------------------------ */
+void orc_measurables(orc_ctx* c, double* tot, double* Ek, double* Ok) {
+    const int N = c->N, NF = c->NF, ns = orc_n_spect(N);
+    const double norm_fac = 0.5 / pow((double)N * N * N, 2.0);
+    const double const_fac = 8.0 * pow(M_PI, 3.0);
+    double s_diss = 0, s_enst = 0, s_pal = 0, s_hel = 0, s_en = 0;
+    if (Ek) memset(Ek, 0, sizeof(double) * ns);
+    if (Ok) memset(Ok, 0, sizeof(double) * ns);
+    const int bug = c->p.bugcompat_measures;
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long indx = (long)(i * N + j) * NF + k;
+                const cplx* u = c->u_hat + 3 * indx;
+                double kx = c->kx[i], ky = c->ky[j], kz = c->kz[k];
+                cplx wx = I * (ky * u[2] - kz * u[1]);
+                cplx wy = I * (kz * u[0] - kx * u[2]);
+                cplx wz = I * (kx * u[1] - ky * u[0]);
+                cplx cx = I * (ky * wz - kz * wy);
+                cplx cy = I * (kz * wx - kx * wz);
+                cplx cz = I * (kx * wy - ky * wx);
+                double k2 = kx * kx + ky * ky + kz * kz;
+                double pre = c->p.visc_pow == 2 ? c->p.nu * k2 * k2 : c->p.nu * k2;
+                double ux2 = cabs(u[0] * conj(u[0])), uy2 = cabs(u[1] * conj(u[1])), uz2 = cabs(u[2] * conj(u[2]));
+                double wx2 = cabs(wx * conj(wx)), wy2 = cabs(wy * conj(wy)), wz2 = cabs(wz * conj(wz));
+                double cx2 = cabs(cx * conj(cx)), cy2 = cabs(cy * conj(cy)), cz2 = cabs(cz * conj(cz));
+                /* D12: the reference's Re(u.w) (solver.c:1227) is identically zero since
+                 * u.(k x u) = 0; the Parseval form of the helicity conjugates w. */
+                double hel = bug ? creal(u[0] * wx + u[1] * wy + u[2] * wz)
+                                 : creal(u[0] * conj(wx) + u[1] * conj(wy) + u[2] * conj(wz));
+                if (k == 0 || k == NF - 1) {
+                    s_diss += pre * (ux2 + uy2 + uz2);
+                    s_enst += wx2 + wy2 + wz2;
+                    s_pal += cx2 + cy2 + cz2;
+                    s_hel += hel;
+                    s_en += ux2 + uy2 + uz2;
+                } else if (bug) {
+                    s_diss += 2.0 * pre * (ux2 + uy2 + uz2);
+                    s_enst += 2.0 * wx2 + wy2 + wz2;
+                    s_pal += 2.0 * cx2 + cy2 + cz2;
+                    s_hel += 2.0 * hel;
+                    s_en += 2.0 * ux2 + uy2 + uz2;
+                } else {
+                    s_diss += 2.0 * pre * (ux2 + uy2 + uz2);
+                    s_enst += 2.0 * (wx2 + wy2 + wz2);
+                    s_pal += 2.0 * (cx2 + cy2 + cz2);
+                    s_hel += 2.0 * hel;
+                    s_en += 2.0 * (ux2 + uy2 + uz2);
+                }
+                int b = (int)round(sqrt(k2));
+                double m = (k == 0 || k == NF - 1) ? 1.0 : 2.0;
+                if (Ek) Ek[b] += m * const_fac * norm_fac * (ux2 + uy2 + uz2);
+                if (Ok) Ok[b] += m * const_fac * norm_fac * (wx2 + wy2 + wz2);
+            }
+    tot[0] = s_en * const_fac * norm_fac;
+    tot[1] = s_enst * const_fac * norm_fac;
+    tot[2] = s_pal * const_fac * norm_fac;
+    tot[3] = s_hel * const_fac * norm_fac;
+    tot[4] = s_diss * 2.0 * const_fac * norm_fac;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Initial conditions, solver.c:1537-1648 (D3 fixed: if / else-if chain)     */
+/* ------------------------------------------------------------------------ */
+static uint64_t splitmix64(uint64_t x) {
+    /* SplitMix64 (Steele, Lea & Flood, OOPSLA 2014) finaliser on x + golden gamma */
+    uint64_t z = x + 0x9E3779B97F4A7C15ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    return z ^ (z >> 31);
+}
+static double uniform01(uint64_t key, uint64_t id, int r) {
+    return (double)(splitmix64(key ^ (id * 8u + (uint64_t)r)) >> 11) * 0x1.0p-53;
+}
+
+int orc_ic(orc_ctx* c, const char* name, uint64_t seed, double k0, double energy) {
+    const int N = c->N, NF = c->NF;
+    cplx* uh = c->u_hat;
+    double* u = c->vel;
+    if (!strcmp(name, "TAYLOR_GREEN")) {
+        /* solver.c:1557-1573, KAPPA = 1 */
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int k = 0; k < N; ++k) {
+                    long indx = (long)(i * N + j) * (N + 2) + k;
+                    u[3 * indx + 0] = sin(c->x[i]) * cos(c->x[j]) * cos(c->x[k]);
+                    u[3 * indx + 1] = -cos(c->x[i]) * sin(c->x[j]) * cos(c->x[k]);
+                    u[3 * indx + 2] = 0.0;
+                }
+        orc_fft_r2c(c, u, (double*)uh);
+    } else if (!strcmp(name, "SHAPIRO")) {
+        /* solver.c:1579-1599 with A = 2, K = L = M = 2 (data_types.h:138-142), t = 0.
+         * D13 fixed: the w component is A cos(Kx) cos(Ly) sin(Mz) (Shapiro 1993);
+         * the reference's cos(Mz) (solver.c:1593, 1686) is neither solenoidal nor
+         * a Beltrami field, so it is not an exact solution. */
+        const double A = 2.0, K = 2.0, L = 2.0, M = 2.0;
+        const double lam = sqrt(K * K + L * L + M * M);
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int k = 0; k < N; ++k) {
+                    long indx = (long)(i * N + j) * (N + 2) + k;
+                    double x = c->x[i], y = c->x[j], z = c->x[k];
+                    u[3 * indx + 0] = -A / (K * K + L * L) * (lam * L * cos(K * x) * sin(L * y) * sin(M * z) + M * K * sin(K * x) * cos(L * y) * cos(M * z));
+                    u[3 * indx + 1] = A / (K * K + L * L) * (lam * K * sin(K * x) * cos(L * y) * sin(M * z) - M * L * cos(K * x) * sin(L * y) * cos(M * z));
+                    u[3 * indx + 2] = A * cos(K * x) * cos(L * y) * (c->p.bugcompat_measures ? cos(M * z) : sin(M * z));
+                }
+        orc_fft_r2c(c, u, (double*)uh);
+    } else if (!strcmp(name, "SPECTRUM")) {
+        /* New component: seeded random-phase solenoidal field with
+         * E(k) ~ k^4 exp(-2 (k/k0)^2), Hermitian on the kz = 0 plane, scaled
+         * to the requested energy. */
+        const long kc2 = (long)(N / 3) * (N / 3);
+        const uint64_t key = splitmix64(seed);
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int k = 0; k < NF; ++k) {
+                    long indx = (long)(i * N + j) * NF + k;
+                    int kx = c->kx[i], ky = c->ky[j], kz = c->kz[k];
+                    long k2 = (long)kx * kx + (long)ky * ky + (long)kz * kz;
+                    cplx* o = uh + 3 * indx;
+                    o[0] = o[1] = o[2] = 0.0;
+                    if (k2 == 0 || k2 > kc2) continue;
+                    int conj_of = 0;
+                    int ci = i, cj = j;
+                    if (kz == 0 && !(kx > 0 || (kx == 0 && ky > 0))) {
+                        conj_of = 1;
+                        ci = (N - i) % N;
+                        cj = (N - j) % N;
+                    }
+                    uint64_t id = (uint64_t)((long)(ci * N + cj) * NF + k);
+                    cplx v[3];
+                    for (int d = 0; d < 3; ++d)
+                        v[d] = (2.0 * uniform01(key, id, 2 * d) - 1.0) + I * (2.0 * uniform01(key, id, 2 * d + 1) - 1.0);
+                    double ckx = c->kx[ci], cky = c->ky[cj], ckz = kz;
+                    cplx kv = ckx * v[0] + cky * v[1] + ckz * v[2];
+                    double kk = (double)k2;
+                    v[0] -= ckx * kv / kk;
+                    v[1] -= cky * kv / kk;
+                    v[2] -= ckz * kv / kk;
+                    double vn = sqrt(creal(v[0] * conj(v[0])) + creal(v[1] * conj(v[1])) + creal(v[2] * conj(v[2])));
+                    if (!(vn > 1e-300)) continue;
+                    double amp = sqrt(kk) * exp(-kk / (k0 * k0)) / vn;
+                    for (int d = 0; d < 3; ++d) o[d] = conj_of ? conj(amp * v[d]) : amp * v[d];
+                }
+        double tot[5];
+        orc_measurables(c, tot, NULL, NULL);
+        double target = 8.0 * pow(M_PI, 3.0) * energy;
+        if (tot[0] > 0.0) {
+            double s = sqrt(target / tot[0]);
+            for (long n = 0; n < 3 * c->nF; ++n) uh[n] *= s;
+        }
+    } else if (!strcmp(name, "TESTING")) {
+        /* solver.c:1600-1604: no field is set */
+        memset(uh, 0, sizeof(cplx) * 3 * (size_t)c->nF);
+    } else {
+        /* RANDOM and unrecognised names: solver.c:1606-1625 with srand(123456789), D6 kept */
+        srand(123456789);
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int k = 0; k < NF; ++k) {
+                    long indx = (long)(i * N + j) * NF + k;
+                    for (int d = 0; d < 3; ++d) {
+                        double a = (double)rand() / (double)RAND_MAX;
+                        double ph = (double)rand() / (double)RAND_MAX;
+                        uh[3 * indx + d] = a * cexp(ph * 2.0 * M_PI * I);
+                    }
+                }
+    }
+    orc_dealias(c, (double*)uh, 3);
+    c->t = c->p.t0;
+    c->dt = c->p.dt;
+    c->iters = 0;
+    if (c->p.forcing == ORC_FORCE_SHELL) c->force_target = energy_shells(c, uh, c->p.force_k);
+    return 0;
+}
+
+/* Real-space u and w, normalised by 1/N^3 (hdf5_funcs.c:586-600, 662-676) */
+void orc_real_space(orc_ctx* c, double* u, double* w) {
+    const int N = c->N, NF = c->NF;
+    const double s = 1.0 / ((double)N * N * N);
+    if (u) {
+        orc_fft_c2r(c, (const double*)c->u_hat, u);
+        for (long n = 0; n < 3 * c->nR; ++n) u[n] *= s;
+    }
+    if (w) {
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j)
+                for (int k = 0; k < NF; ++k) {
+                    long indx = (long)(i * N + j) * NF + k;
+                    const cplx* v = c->u_hat + 3 * indx;
+                    c->w_hat[3 * indx + 0] = I * (c->ky[j] * v[2] - c->kz[k] * v[1]);
+                    c->w_hat[3 * indx + 1] = I * (c->kz[k] * v[0] - c->kx[i] * v[2]);
+                    c->w_hat[3 * indx + 2] = I * (c->kx[i] * v[1] - c->ky[j] * v[0]);
+                }
+        orc_fft_c2r(c, (const double*)c->w_hat, w);
+        for (long n = 0; n < 3 * c->nR; ++n) w[n] *= s;
+    }
+}
