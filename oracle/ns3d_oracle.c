@@ -622,8 +622,12 @@ void orc_measurables(orc_ctx* c, double* tot, double* Ek, double* Ok) {
                     s_hel += 2.0 * hel;
                     s_en += 2.0 * (ux2 + uy2 + uz2);
                 }
+                /* D14: round(|k|) reaches n_spect for the corner modes when the
+                 * fraction of sqrt(3)N/2 is >= 1/2 (e.g. N = 8); the reference
+                 * writes past the end there (solver.c:1242-1250). Dropped here. */
                 int b = (int)round(sqrt(k2));
                 double m = (k == 0 || k == NF - 1) ? 1.0 : 2.0;
+                if (b >= ns) continue;
                 if (Ek) Ek[b] += m * const_fac * norm_fac * (ux2 + uy2 + uz2);
                 if (Ok) Ok[b] += m * const_fac * norm_fac * (wx2 + wy2 + wz2);
             }
