@@ -36,7 +36,7 @@ EXPORTS = (
     "ns3d_step", "ns3d_step_host", "ns3d_rhs_host", "ns3d_dealias_host", "ns3d_measurables",
     "ns3d_real_space_host", "ns3d_get_time", "ns3d_set_time", "ns3d_get_forcing_target",
     "ns3d_set_forcing_target", "ns3d_max_speed_sum", "ns3d_stream", "ns3d_kernels_per_step",
-    "ns3d_last_step_ms", "ns3d_profile_step",
+    "ns3d_last_step_ms", "ns3d_profile_step", "ns3d_measurables_noalloc",
 )
 
 

@@ -122,6 +122,19 @@ ns3d_status ns3d_measurables(ns3d_ctx* ctx, ns3d_measures* out, double* Ek, doub
  * 662-676), reference real layout; either pointer may be NULL. */
 ns3d_status ns3d_real_space_host(ns3d_ctx* ctx, double* u, double* w);
 
+/* ComputeSystemMeasurables for callers that cannot allocate device memory
+ * (no counterpart in the reference). Input: a device array in the reference
+ * Fourier layout, complex double [N][N][N/2+1][3]; every mode counts, as in
+ * the reference. Outputs (device): d_totals[5] in the order of ns3d_measures,
+ * and n_spect doubles each in d_Ek / d_Ok (either may be NULL). Runs
+ * asynchronously on `stream` (NULL = default stream). Its partial sums live in
+ * a 2 MiB static device array shared by every call, so N <= 512 (larger N:
+ * NS3D_ERR_INVALID) and calls that overlap on the GPU race. The first call on
+ * a device resolves that array's address; make it before any stream capture.
+ * Allocates nothing. */
+ns3d_status ns3d_measurables_noalloc(int N, double nu, int visc_pow, const double* d_u_hat,
+                                     double* d_totals, double* d_Ek, double* d_Ok, void* stream);
+
 /* Time bookkeeping (solver.c:1314-1363): current t, dt and completed steps. */
 ns3d_status ns3d_get_time(ns3d_ctx* ctx, double* t, double* dt, long* iters);
 ns3d_status ns3d_set_time(ns3d_ctx* ctx, double t, double dt, long iters);
