@@ -85,10 +85,12 @@ class Impl final : public Base {
         *sd_host_ = sd;
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
         // opt-in shared memory sizes
-        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
+        if constexpr (zline_ok<T, N>())
+            NS3D_CK(cudaFuncSetAttribute(k_zline<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_zl()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         set_xfwd_attrs<INT_IFRK4>();
@@ -117,12 +119,19 @@ class Impl final : public Base {
     }
 
     void p1(const cx<T>* in) {
-        k_xinv<T, N><<<dim3(NTA, G::NKY), TA * PA::P, smem_a(), s_>>>(in, W_, tw_);
+        k_xinv<T, N><<<dim3(NTX, G::NKY), TX * PX::P, smem_x(), s_>>>(in, W_, tw_);
     }
     void p2() { k_ypass<T, N, true><<<dim3(NTA, N, 6), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
+    static constexpr size_t smem_zl() { return sizeof(cx<T>) * (size_t)ZLINE_WARPS * (32 / PA::P) * zpad<N>(); }
     void p3(int want_umax) {
-        k_zpass<T, N, 0><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
-            W_, tw_, nullptr, &sd_->umax_bits, want_umax);
+        if constexpr (zline_ok<T, N>()) {
+            constexpr long long lines_per_cta = ZLINE_WARPS * (32 / PA::P);
+            k_zline<T, N><<<(unsigned)((long long)N * N / lines_per_cta), ZLINE_WARPS * 32, smem_zl(), s_>>>(
+                W_, tw_, &sd_->umax_bits, want_umax);
+        } else {
+            k_zpass<T, N, 0><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+                W_, tw_, nullptr, &sd_->umax_bits, want_umax);
+        }
     }
     void p4() { k_ypass<T, N, false><<<dim3(NTA, N, 3), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
     template <int INTEG, int MODE>
@@ -200,7 +209,7 @@ class Impl final : public Base {
 
     // per-kernel-class timing of `reps` steps launched one kernel at a time
     ns3d_status profile(int reps, const char** names, float* ms, double* bytes, int maxc, int* count) override {
-        static const char* kNames[6] = {"k_xinv", "k_ypass_inv", "k_zpass", "k_ypass_fwd", "k_xfwd", "k_misc"};
+        static const char* kNames[6] = {"k_xinv", "k_ypass_inv", zline_ok<T, N>() ? "k_zline" : "k_zpass", "k_ypass_fwd", "k_xfwd", "k_misc"};
         std::vector<cudaEvent_t> ev(2 * 6 * 4 + 2);
         for (auto& e : ev) NS3D_CK(cudaEventCreate(&e));
         double acc[6] = {0, 0, 0, 0, 0, 0};

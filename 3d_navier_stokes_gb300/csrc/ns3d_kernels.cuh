@@ -66,7 +66,9 @@ template <typename T, int N> constexpr int tile_a() {
     return sizeof(T) == 4 ? (Plans<N>::A::P * 16 <= 512 ? 16 : 8) : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
 }
 template <typename T, int N> constexpr int tile_x() {
-    return sizeof(T) == 4 ? (Plans<N>::X::P * 16 <= 512 ? 16 : 8) : (Plans<N>::X::P * 8 <= 256 ? 8 : 4);
+    constexpr int P = Plans<N>::X::P;
+    return sizeof(T) == 4 ? (P * 16 <= 512 ? 16 : (P * 8 <= 512 ? 8 : 4))
+                          : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
 }
 // line pairs per CTA of the z pass (>= 96 threads)
 template <int N> constexpr int zpairs() {
@@ -103,15 +105,17 @@ enum { INT_IFRK4 = 0, INT_RK4CN = 1 };
 enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAIN = 9 };
 
 // ---------------------------------------------------------------------------
-// P1: inverse FFT along kx with curl-on-load.
-// grid (ntile, NKY); block TT*P; smem N*TT complex.
+// P1: inverse FFT along kx with curl-on-load. grid (ntile, NKY); block
+// TT*P; smem N*TT complex. The three velocity components of a pencil block
+// are loaded up front; the kx-weighted inputs of the vorticity are formed in
+// registers, so the five transforms below read each input once.
 // ---------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void __launch_bounds__(tile_a<T, N>() * Plans<N>::A::P)
+__global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
 k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
-    using PL = typename Plans<N>::A;
-    constexpr int TT = tile_a<T, N>();
+    using PL = typename Plans<N>::X;
+    constexpr int TT = tile_x<T, N>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -130,19 +134,17 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     StridedIdx<TT> sidx{t};
     SyncBlock sync;
 
-    auto load = [&](int c, cx<T>(&v)[E], bool ikx) {
+    auto load = [&](int c, cx<T>(&v)[E]) {
         const cx<T>* src = U + (long long)c * G::FS + off;
 #pragma unroll
         for (int s = 0; s < E; ++s) {
-            const int i = p + P * s;
-            const int kx = kof<N>(i);
-            cx<T> a = czero<T>();
-            if (colok && kx * kx <= rem) {
-                a = src[(long long)i * xs] * scale;
-                if (ikx) a = mul_i(a) * T(kx);
-            }
-            v[s] = a;
+            const int kx = kof<N>(p + P * s);
+            v[s] = (colok && kx * kx <= rem) ? src[(long long)(p + P * s) * xs] * scale : czero<T>();
         }
+    };
+    auto ikx = [&](const cx<T>(&v)[E], cx<T>(&o)[E]) {
+#pragma unroll
+        for (int s = 0; s < E; ++s) o[s] = mul_i(v[s]) * T(kof<N>(p + P * s));
     };
     auto store = [&](int f, const cx<T>(&v)[E]) {
         if (!colok) return;
@@ -151,37 +153,34 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
         for (int s = 0; s < E; ++s) dst[(long long)(p + P * s) * xs] = v[s];
     };
 
-    cx<T> A[E], B[E];
+    cx<T> X[E], Y[E], Z[E], B[E];
+    load(0, X);
+    load(1, Y);
+    load(2, Z);
     const T fky = T(ky), fkz = T(kz);
-    // ux, kept as Tx
-    load(0, A, false);
-    PL::inv(A, sbuf, p, tw, sidx, sync);
-    store(0, A);
-    // wz = T(i kx uy) - i ky Tx
-    load(1, B, true);
+    // wz = T(i kx uy) - i ky T(ux)
+    ikx(Y, B);
     PL::inv(B, sbuf, p, tw, sidx, sync);
+    PL::inv(X, sbuf, p, tw, sidx, sync);
+    store(0, X);
 #pragma unroll
-    for (int s = 0; s < E; ++s) B[s] = B[s] - mul_i(A[s]) * fky;
+    for (int s = 0; s < E; ++s) B[s] = B[s] - mul_i(X[s]) * fky;
     store(5, B);
-    // wy = i kz Tx - T(i kx uz)
-    load(2, B, true);
+    // wy = i kz T(ux) - T(i kx uz)
+    ikx(Z, B);
     PL::inv(B, sbuf, p, tw, sidx, sync);
 #pragma unroll
-    for (int s = 0; s < E; ++s) B[s] = mul_i(A[s]) * fkz - B[s];
+    for (int s = 0; s < E; ++s) B[s] = mul_i(X[s]) * fkz - B[s];
     store(4, B);
-    // uy, kept as Ty
-    load(1, A, false);
-    PL::inv(A, sbuf, p, tw, sidx, sync);
-    store(1, A);
-    // uz, then wx = i ky Tz - i kz Ty
-    load(2, B, false);
-    PL::inv(B, sbuf, p, tw, sidx, sync);
-    store(2, B);
+    // uy, uz, then wx = i ky T(uz) - i kz T(uy)
+    PL::inv(Y, sbuf, p, tw, sidx, sync);
+    store(1, Y);
+    PL::inv(Z, sbuf, p, tw, sidx, sync);
+    store(2, Z);
 #pragma unroll
-    for (int s = 0; s < E; ++s) B[s] = mul_i(B[s]) * fky - mul_i(A[s]) * fkz;
+    for (int s = 0; s < E; ++s) B[s] = mul_i(Z[s]) * fky - mul_i(Y[s]) * fkz;
     store(3, B);
 }
-
 // ---------------------------------------------------------------------------
 // P2 / P4: FFT along y, in place. grid (ntile, N, nfields).
 // Inverse: inputs only where ky^2 + kz^2 <= KC^2, outputs every y.
@@ -381,6 +380,118 @@ k_zpass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, T* __restrict__ rea
 }
 
 // ---------------------------------------------------------------------------
+// P3, line-per-group form (FP32, P <= 32): a group of P = N/E lanes inside one
+// warp owns a whole z line. It runs the three inverse complex FFTs
+// (ux + i uy, uz + i wx, wy + i wz), keeps all six real fields in registers,
+// forms u x w there, and runs two forward FFTs: Nx + i Ny (separated through
+// the group's exchange buffer) and Nz alone (a real input, whose first KC+1
+// outputs are the spectrum directly). All exchanges are warp-synchronous, so
+// warps never wait on each other.
+// ---------------------------------------------------------------------------
+struct SyncWarp {
+    __device__ __forceinline__ void operator()() const { __syncwarp(); }
+};
+constexpr int ZLINE_WARPS = 4;
+
+template <typename T, int N>
+constexpr bool zline_ok() {
+    return sizeof(T) == 4 && Plans<N>::A::P <= 32 && (32 % Plans<N>::A::P) == 0 && Plans<N>::A::E <= 16 &&
+           ((long long)N * N) % (ZLINE_WARPS * (32 / Plans<N>::A::P)) == 0;
+}
+
+template <typename T, int N>
+__global__ void __launch_bounds__(ZLINE_WARPS * 32)
+k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, unsigned long long* __restrict__ umax_bits,
+        int want_umax) {
+    using G = Geo<N>;
+    using PL = typename Plans<N>::A;
+    constexpr int E = PL::E, P = PL::P, GPW = 32 / P;
+    constexpr int XS = zpad<N>();
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int p = lane % P, gi = lane / P;
+    const long long line = ((long long)blockIdx.x * ZLINE_WARPS + warp) * GPW + gi;
+    cx<T>* sb = reinterpret_cast<cx<T>*>(smem_raw) + (warp * GPW + gi) * XS;
+    PaddedIdx sidx;
+    SyncWarp sync;
+
+    auto load_pair = [&](int f, cx<T>(&v)[E]) {
+        const cx<T>* A = W + (long long)f * G::FS + line * G::NZP;
+        const cx<T>* B = A + G::FS;
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int m = p + P * s;
+            cx<T> z = czero<T>();
+            if (m == 0) {
+                z = mk(A[0].x, B[0].x);
+            } else if (m <= G::KC) {
+                const cx<T> a = A[m], b = B[m];
+                z = mk(a.x - b.y, a.y + b.x);
+            } else if (m >= N - G::KC) {
+                const cx<T> a = A[N - m], b = B[N - m];
+                z = mk(a.x + b.y, b.x - a.y);
+            }
+            v[s] = z;
+        }
+    };
+
+    // all loads first: three times the bytes in flight before the first FFT
+    cx<T> V1[E], V2[E], V3[E];
+    load_pair(0, V1);
+    load_pair(2, V2);
+    load_pair(4, V3);
+    PL::inv(V1, sb, p, tw, sidx, sync);
+    PL::inv(V2, sb, p, tw, sidx, sync);
+    PL::inv(V3, sb, p, tw, sidx, sync);
+
+    T um = T(0);
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+        const T ux = V1[s].x, uy = V1[s].y, uz = V2[s].x;
+        const T wx = V2[s].y, wy = V3[s].x, wz = V3[s].y;
+        um = fmaxf(um, fabsf(ux) + fabsf(uy) + fabsf(uz));
+        V1[s] = mk(uy * wz - uz * wy, uz * wx - ux * wz);
+        V2[s] = mk(ux * wy - uy * wx, T(0));
+    }
+    if (want_umax) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) um = fmaxf(um, __shfl_xor_sync(0xffffffffu, um, o));
+        if (lane == 0) Bits<T>::amax(umax_bits, um);
+    }
+
+    // Nx + i Ny -> two spectra through the exchange buffer
+    PL::fwd(V1, sb, p, tw, sidx, sync);
+#pragma unroll
+    for (int s = 0; s < E; ++s) sb[sidx(p + P * s)] = V1[s];
+    __syncwarp();
+    {
+        cx<T>* outA = W + line * G::NZP;
+        cx<T>* outB = outA + G::FS;
+        const T half = T(0.5);
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int m = p + P * s;
+            if (m <= G::KC) {
+                const cx<T> zm = sb[sidx(m)];
+                const cx<T> zc = conjg(sb[sidx((N - m) % N)]);
+                const cx<T> sum = zm + zc, dif = zm - zc;
+                outA[m] = sum * half;
+                outB[m] = mk(dif.y * half, -dif.x * half);
+            }
+        }
+    }
+    __syncwarp();
+    // Nz (real input): its spectrum is the transform itself
+    PL::fwd(V2, sb, p, tw, sidx, sync);
+    cx<T>* outC = W + 2 * G::FS + line * G::NZP;
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+        const int m = p + P * s;
+        if (m <= G::KC) outC[m] = V2[s];
+    }
+}
+
+// ---------------------------------------------------------------------------
 // P5: forward FFT along x of the 3 product fields, then per mode the Leray
 // projection, dealias mask and RK stage update. grid (ntile, NKY).
 // tab[k2] holds (E_half, E_full) for IF-RK4 or (a, b) = ((2-D)/(2+D),
@@ -415,8 +526,9 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         const cx<T>* src = W + (long long)c * G::FS + off;
 #pragma unroll
         for (int s = 0; s < E; ++s) F[c][s] = colok ? src[(long long)(p + P * s) * xs] : czero<T>();
-        PL::fwd(F[c], sbuf, p, tw, sidx, sync);
     }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) PL::fwd(F[c], sbuf, p, tw, sidx, sync);
     if (!colok) return;
 
     T h = T(0);
