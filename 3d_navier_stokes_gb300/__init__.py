@@ -21,7 +21,7 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_build", "libns3d.so")
+LIB_PATH = os.path.join(os.environ.get("NS3D_BUILD_DIR") or os.path.join(_HERE, "_build"), "libns3d.so")
 _lib = None
 
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NUMERIC, ERR_TIMEOUT = range(7)

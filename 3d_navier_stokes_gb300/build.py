@@ -16,13 +16,14 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
-OUT = os.path.join(HERE, "_build")
+OUT = os.environ.get("NS3D_BUILD_DIR") or os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libns3d.so")
 ROOT = os.path.dirname(HERE)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr",
-              "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")] + ARCH
+              "-Xcompiler", "-fPIC,-O2", "-I", os.path.join(ROOT, "include")] + ARCH + \
+    os.environ.get("NS3D_NVCC_EXTRA", "").split()
 
 
 def _nvcc() -> str:

@@ -89,8 +89,14 @@ class Impl final : public Base {
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
-        if constexpr (zline_ok<T, N>())
+        if constexpr (zline_ok<T, N>()) {
             NS3D_CK(cudaFuncSetAttribute(k_zline<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_zl()));
+            int per_sm = 0, nsm = 0, dev = 0;
+            NS3D_CK(cudaGetDevice(&dev));
+            NS3D_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            NS3D_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_zline<T, N>, ZLINE_WARPS * 32, smem_zl()));
+            zline_ctas_ = (per_sm > 0 ? per_sm : 1) * nsm;
+        }
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         set_xfwd_attrs<INT_IFRK4>();
@@ -122,12 +128,14 @@ class Impl final : public Base {
         k_xinv<T, N><<<dim3(NTX, G::NKY), TX * PX::P, smem_x(), s_>>>(in, W_, tw_);
     }
     void p2() { k_ypass<T, N, true><<<dim3(NTA, N, 6), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
-    static constexpr size_t smem_zl() { return sizeof(cx<T>) * (size_t)ZLINE_WARPS * (32 / PA::P) * zpad<N>(); }
+    static constexpr size_t smem_zl() { return zline_smem<T, N>(); }
     void p3(int want_umax) {
         if constexpr (zline_ok<T, N>()) {
-            constexpr long long lines_per_cta = ZLINE_WARPS * (32 / PA::P);
-            k_zline<T, N><<<(unsigned)((long long)N * N / lines_per_cta), ZLINE_WARPS * 32, smem_zl(), s_>>>(
-                W_, tw_, &sd_->umax_bits, want_umax);
+            // persistent: as many CTAs as fit on the device, never more than there are warp tasks
+            const long long groups = (long long)N * N / zline_gpw<N>();
+            long long grid = (long long)zline_ctas_;
+            if (grid * ZLINE_WARPS > groups) grid = (groups + ZLINE_WARPS - 1) / ZLINE_WARPS;
+            k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(W_, tw_, sd_, want_umax);
         } else {
             k_zpass<T, N, 0><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
                 W_, tw_, nullptr, &sd_->umax_bits, want_umax);
@@ -195,6 +203,10 @@ class Impl final : public Base {
         NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         NS3D_CK(cudaGetLastError());
+        if (sd_host_->status == kStatusTimeout) {
+            set_err("a bounded wait for an asynchronous copy gave up at step %lld", sd_host_->iters);
+            return NS3D_ERR_TIMEOUT;
+        }
         if (sd_host_->status != 0) {
             set_err("numeric health check failed at step %lld (NaN/Inf energy or speed)", sd_host_->iters);
             return NS3D_ERR_NUMERIC;
@@ -528,6 +540,7 @@ class Impl final : public Base {
     StepDev* sd_host_ = nullptr;
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
+    int zline_ctas_ = 1;
 };
 
 }  // namespace ns3d

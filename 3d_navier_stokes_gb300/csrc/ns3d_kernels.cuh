@@ -26,6 +26,7 @@
 // FFT(u x w)/N^6 directly.
 #pragma once
 #include "fft_engine.cuh"
+#include "tma.cuh"
 
 namespace ns3d {
 
@@ -62,12 +63,19 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 
 // Tile width (pencils per CTA along kz) of the strided passes: one 128-byte
 // row segment per pencil row where the thread count allows.
+#ifndef NS3D_TILE_A32
+#define NS3D_TILE_A32 8
+#endif
+#ifndef NS3D_TILE_X32
+#define NS3D_TILE_X32 16
+#endif
 template <typename T, int N> constexpr int tile_a() {
-    return sizeof(T) == 4 ? (Plans<N>::A::P * 16 <= 512 ? 16 : 8) : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
+    return sizeof(T) == 4 ? (Plans<N>::A::P * NS3D_TILE_A32 <= 512 ? NS3D_TILE_A32 : 8)
+                          : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
 }
 template <typename T, int N> constexpr int tile_x() {
     constexpr int P = Plans<N>::X::P;
-    return sizeof(T) == 4 ? (P * 16 <= 512 ? 16 : (P * 8 <= 512 ? 8 : 4))
+    return sizeof(T) == 4 ? (P * NS3D_TILE_X32 <= 512 ? NS3D_TILE_X32 : (P * 8 <= 512 ? 8 : 4))
                           : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
 }
 // line pairs per CTA of the z pass (>= 96 threads)
@@ -380,13 +388,16 @@ k_zpass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, T* __restrict__ rea
 }
 
 // ---------------------------------------------------------------------------
-// P3, line-per-group form (FP32, P <= 32): a group of P = N/E lanes inside one
-// warp owns a whole z line. It runs the three inverse complex FFTs
-// (ux + i uy, uz + i wx, wy + i wz), keeps all six real fields in registers,
-// forms u x w there, and runs two forward FFTs: Nx + i Ny (separated through
-// the group's exchange buffer) and Nz alone (a real input, whose first KC+1
-// outputs are the spectrum directly). All exchanges are warp-synchronous, so
-// warps never wait on each other.
+// P3, line-per-group form (FP32, P <= 32), persistent and fed by bulk
+// asynchronous copies. A group of P = N/E lanes inside one warp owns a z line.
+// Each warp walks its own sequence of line groups; lane 0 copies the next
+// group's six field lines (cp.async.bulk, completion on an mbarrier) into the
+// other half of a two-stage shared-memory buffer while the warp transforms the
+// current group: three inverse complex FFTs (ux + i uy, uz + i wx, wy + i wz),
+// u x w on the six real fields held in registers, then two forward FFTs:
+// Nx + i Ny (separated through the group's exchange buffer) and Nz alone (a
+// real input, whose first KC+1 outputs are the spectrum directly). Exchanges
+// are warp-synchronous, so warps never wait on each other.
 // ---------------------------------------------------------------------------
 struct SyncWarp {
     __device__ __forceinline__ void operator()() const { __syncwarp(); }
@@ -396,101 +407,150 @@ constexpr int ZLINE_WARPS = 4;
 template <typename T, int N>
 constexpr bool zline_ok() {
     return sizeof(T) == 4 && Plans<N>::A::P <= 32 && (32 % Plans<N>::A::P) == 0 && Plans<N>::A::E <= 16 &&
-           ((long long)N * N) % (ZLINE_WARPS * (32 / Plans<N>::A::P)) == 0;
+           ((long long)N * N) % (32 / Plans<N>::A::P) == 0;
+}
+template <int N> constexpr int zline_gpw() { return 32 / Plans<N>::A::P; }
+// complex elements of shared memory per warp: 2 stages x GPW lines x 6 fields x NZP, plus the
+// GPW exchange buffers, rounded up to 16 elements
+template <typename T, int N> constexpr int zline_warp_elems() {
+    return (2 * zline_gpw<N>() * 6 * Geo<N>::NZP + zline_gpw<N>() * zpad<N>() + 15) / 16 * 16;
+}
+template <typename T, int N> constexpr size_t zline_smem() {
+    return sizeof(cx<T>) * (size_t)ZLINE_WARPS * zline_warp_elems<T, N>() + 16 * ZLINE_WARPS;
 }
 
 template <typename T, int N>
 __global__ void __launch_bounds__(ZLINE_WARPS * 32)
-k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, unsigned long long* __restrict__ umax_bits,
-        int want_umax) {
+k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, int want_umax) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
-    constexpr int E = PL::E, P = PL::P, GPW = 32 / P;
-    constexpr int XS = zpad<N>();
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+    constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>();
+    constexpr int NZP = G::NZP;
+    constexpr long long NG = (long long)N * N / GPW;   // line groups
+    constexpr int SE = GPW * 6 * NZP;                  // elements per stage
+    constexpr uint32_t STAGE_BYTES = SE * sizeof(cx<T>);
+    constexpr uint32_t LINE_BYTES = NZP * sizeof(cx<T>);
+    extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = lane % P, gi = lane / P;
-    const long long line = ((long long)blockIdx.x * ZLINE_WARPS + warp) * GPW + gi;
-    cx<T>* sb = reinterpret_cast<cx<T>*>(smem_raw) + (warp * GPW + gi) * XS;
+    cx<T>* wbase = reinterpret_cast<cx<T>*>(smem_raw) + (size_t)warp * zline_warp_elems<T, N>();
+    cx<T>* stage[2] = {wbase, wbase + SE};
+    cx<T>* sb = wbase + 2 * SE + gi * zpad<N>();
+    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + sizeof(cx<T>) * (size_t)ZLINE_WARPS *
+                                                                zline_warp_elems<T, N>()) + 2 * warp;
     PaddedIdx sidx;
     SyncWarp sync;
 
-    auto load_pair = [&](int f, cx<T>(&v)[E]) {
-        const cx<T>* A = W + (long long)f * G::FS + line * G::NZP;
-        const cx<T>* B = A + G::FS;
-#pragma unroll
-        for (int s = 0; s < E; ++s) {
-            const int m = p + P * s;
-            cx<T> z = czero<T>();
-            if (m == 0) {
-                z = mk(A[0].x, B[0].x);
-            } else if (m <= G::KC) {
-                const cx<T> a = A[m], b = B[m];
-                z = mk(a.x - b.y, a.y + b.x);
-            } else if (m >= N - G::KC) {
-                const cx<T> a = A[N - m], b = B[N - m];
-                z = mk(a.x + b.y, b.x - a.y);
-            }
-            v[s] = z;
+    if (lane == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    __syncwarp();
+    auto issue = [&](long long g, int s) {
+        if (lane == 0) {
+            fence_proxy_async_smem();
+            mbar_arrive_expect_tx(&bars[s], STAGE_BYTES);
+            for (int l = 0; l < GPW; ++l)
+                for (int f = 0; f < 6; ++f)
+                    bulk_g2s(stage[s] + (l * 6 + f) * NZP, W + (long long)f * G::FS + (g * GPW + l) * NZP,
+                             LINE_BYTES, &bars[s]);
         }
     };
 
-    // all loads first: three times the bytes in flight before the first FFT
-    cx<T> V1[E], V2[E], V3[E];
-    load_pair(0, V1);
-    load_pair(2, V2);
-    load_pair(4, V3);
-    PL::inv(V1, sb, p, tw, sidx, sync);
-    PL::inv(V2, sb, p, tw, sidx, sync);
-    PL::inv(V3, sb, p, tw, sidx, sync);
-
+    const long long nw = (long long)gridDim.x * ZLINE_WARPS;
+    long long g = (long long)blockIdx.x * ZLINE_WARPS + warp;
+    uint32_t phase = 0;   // bit s = parity to wait for on stage s
     T um = T(0);
+    int s = 0;
+    if (g < NG) issue(g, 0);
+    for (; g < NG; g += nw, s ^= 1) {
+        const bool more = g + nw < NG;
+        if (more) issue(g + nw, s ^ 1);
+        const bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], (phase >> s) & 1u));
+        phase ^= 1u << s;
+        if (!ok) {
+            // record the timeout, let the copy already issued for the next group land, leave
+            if (more) (void)mbar_wait(&bars[s ^ 1], (phase >> (s ^ 1)) & 1u);
+            if (lane == 0) atomicExch(&sd->status, kStatusTimeout);
+            return;
+        }
+        const cx<T>* in = stage[s] + gi * 6 * NZP;
+        const long long line = g * GPW + gi;
+
+        auto load_pair = [&](int f, cx<T>(&v)[E]) {
+            const cx<T>* A = in + f * NZP;
+            const cx<T>* B = A + NZP;
 #pragma unroll
-    for (int s = 0; s < E; ++s) {
-        const T ux = V1[s].x, uy = V1[s].y, uz = V2[s].x;
-        const T wx = V2[s].y, wy = V3[s].x, wz = V3[s].y;
-        um = fmaxf(um, fabsf(ux) + fabsf(uy) + fabsf(uz));
-        V1[s] = mk(uy * wz - uz * wy, uz * wx - ux * wz);
-        V2[s] = mk(ux * wy - uy * wx, T(0));
+            for (int q = 0; q < E; ++q) {
+                const int m = p + P * q;
+                cx<T> z = czero<T>();
+                if (m == 0) {
+                    z = mk(A[0].x, B[0].x);
+                } else if (m <= G::KC) {
+                    const cx<T> a = A[m], b = B[m];
+                    z = mk(a.x - b.y, a.y + b.x);
+                } else if (m >= N - G::KC) {
+                    const cx<T> a = A[N - m], b = B[N - m];
+                    z = mk(a.x + b.y, b.x - a.y);
+                }
+                v[q] = z;
+            }
+        };
+
+        cx<T> V1[E], V2[E], V3[E];
+        load_pair(0, V1);
+        load_pair(2, V2);
+        load_pair(4, V3);
+        PL::inv(V1, sb, p, tw, sidx, sync);
+        PL::inv(V2, sb, p, tw, sidx, sync);
+        PL::inv(V3, sb, p, tw, sidx, sync);
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const T ux = V1[q].x, uy = V1[q].y, uz = V2[q].x;
+            const T wx = V2[q].y, wy = V3[q].x, wz = V3[q].y;
+            um = fmaxf(um, fabsf(ux) + fabsf(uy) + fabsf(uz));
+            V1[q] = mk(uy * wz - uz * wy, uz * wx - ux * wz);
+            V2[q] = mk(ux * wy - uy * wx, T(0));
+        }
+        // Nx + i Ny -> two spectra through the exchange buffer
+        PL::fwd(V1, sb, p, tw, sidx, sync);
+#pragma unroll
+        for (int q = 0; q < E; ++q) sb[sidx(p + P * q)] = V1[q];
+        __syncwarp();
+        {
+            cx<T>* outA = W + line * NZP;
+            cx<T>* outB = outA + G::FS;
+            const T half = T(0.5);
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int m = p + P * q;
+                if (m <= G::KC) {
+                    const cx<T> zm = sb[sidx(m)];
+                    const cx<T> zc = conjg(sb[sidx((N - m) % N)]);
+                    const cx<T> sum = zm + zc, dif = zm - zc;
+                    outA[m] = sum * half;
+                    outB[m] = mk(dif.y * half, -dif.x * half);
+                }
+            }
+        }
+        __syncwarp();
+        // Nz (real input): its spectrum is the transform itself
+        PL::fwd(V2, sb, p, tw, sidx, sync);
+        cx<T>* outC = W + 2 * G::FS + line * NZP;
+#pragma unroll
+        for (int q = 0; q < E; ++q) {
+            const int m = p + P * q;
+            if (m <= G::KC) outC[m] = V2[q];
+        }
+        __syncwarp();
     }
     if (want_umax) {
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) um = fmaxf(um, __shfl_xor_sync(0xffffffffu, um, o));
-        if (lane == 0) Bits<T>::amax(umax_bits, um);
-    }
-
-    // Nx + i Ny -> two spectra through the exchange buffer
-    PL::fwd(V1, sb, p, tw, sidx, sync);
-#pragma unroll
-    for (int s = 0; s < E; ++s) sb[sidx(p + P * s)] = V1[s];
-    __syncwarp();
-    {
-        cx<T>* outA = W + line * G::NZP;
-        cx<T>* outB = outA + G::FS;
-        const T half = T(0.5);
-#pragma unroll
-        for (int s = 0; s < E; ++s) {
-            const int m = p + P * s;
-            if (m <= G::KC) {
-                const cx<T> zm = sb[sidx(m)];
-                const cx<T> zc = conjg(sb[sidx((N - m) % N)]);
-                const cx<T> sum = zm + zc, dif = zm - zc;
-                outA[m] = sum * half;
-                outB[m] = mk(dif.y * half, -dif.x * half);
-            }
-        }
-    }
-    __syncwarp();
-    // Nz (real input): its spectrum is the transform itself
-    PL::fwd(V2, sb, p, tw, sidx, sync);
-    cx<T>* outC = W + 2 * G::FS + line * G::NZP;
-#pragma unroll
-    for (int s = 0; s < E; ++s) {
-        const int m = p + P * s;
-        if (m <= G::KC) outC[m] = V2[s];
+        if (lane == 0) Bits<T>::amax(&sd->umax_bits, um);
     }
 }
-
 // ---------------------------------------------------------------------------
 // P5: forward FFT along x of the 3 product fields, then per mode the Leray
 // projection, dealias mask and RK stage update. grid (ntile, NKY).
