@@ -66,17 +66,45 @@ def _compile(src: str, nvcc: str, verbose: bool) -> str:
     return obj
 
 
+CC = os.environ.get("CC", "gcc")
+C_FLAGS = ["-std=gnu11", "-O2", "-fPIC", "-Wall", "-I", os.path.join(ROOT, "include")]
+DRIVER = os.path.join(HERE, "driver", "solver_main.c")
+SOLVER = os.path.join(OUT, "solver")
+
+
+def _compile_c(src: str, verbose: bool) -> str:
+    obj = os.path.join(OUT, os.path.basename(src)[:-2] + ".c.o")
+    newest = max([os.path.getmtime(src)] + [os.path.getmtime(h) for h in _headers()])
+    if os.path.exists(obj) and os.path.getmtime(obj) >= newest:
+        return obj
+    cmd = [CC] + C_FLAGS + ["-c", src, "-o", obj]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"{CC} failed on {src}:\n{r.stdout}\n{r.stderr}")
+    return obj
+
+
 def build(verbose: bool = False) -> str:
+    """Build libns3d.so (CUDA + C units) and the `solver` driver; return the library path."""
     os.makedirs(OUT, exist_ok=True)
     nvcc = _nvcc()
     srcs = _sources()
+    csrcs = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".c"))
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(srcs), os.cpu_count() or 4))) as ex:
         objs = list(ex.map(lambda s: _compile(s, nvcc, verbose), srcs))
+    objs += [_compile_c(s, verbose) for s in csrcs]
     if not os.path.exists(LIB) or max(os.path.getmtime(o) for o in objs) > os.path.getmtime(LIB):
         cmd = [nvcc] + ARCH + ["-shared", "--cudart", "static", "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if not os.path.exists(SOLVER) or max(os.path.getmtime(DRIVER), os.path.getmtime(LIB)) > os.path.getmtime(SOLVER):
+        cmd = [CC] + C_FLAGS + [DRIVER, "-o", SOLVER, "-L", OUT, "-lns3d", "-lm", "-Wl,-rpath,$ORIGIN"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver link failed:\n{r.stdout}\n{r.stderr}")
     return LIB
 
 
