@@ -37,6 +37,10 @@ EXPORTS = (
     "ns3d_real_space_host", "ns3d_get_time", "ns3d_set_time", "ns3d_get_forcing_target",
     "ns3d_set_forcing_target", "ns3d_max_speed_sum", "ns3d_stream", "ns3d_kernels_per_step",
     "ns3d_last_step_ms", "ns3d_profile_step", "ns3d_measurables_noalloc",
+    "ns3d_ensemble_create", "ns3d_ensemble_destroy", "ns3d_ensemble_last_error",
+    "ns3d_ensemble_initial_condition", "ns3d_ensemble_set_state_host", "ns3d_ensemble_get_state_host",
+    "ns3d_ensemble_measurables", "ns3d_ensemble_get_time", "ns3d_ensemble_step", "ns3d_ensemble_info",
+    "ns3d_ensemble_last_step_ms",
 )
 
 
@@ -136,6 +140,28 @@ def lib():
         L.ns3d_profile_step.restype = I
         L.ns3d_profile_step.argtypes = [P, I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_float),
                                         D, I, ctypes.POINTER(I)]
+        L.ns3d_ensemble_create.restype = I
+        L.ns3d_ensemble_create.argtypes = [ctypes.POINTER(Params), I, ctypes.POINTER(P)]
+        L.ns3d_ensemble_destroy.restype = I
+        L.ns3d_ensemble_destroy.argtypes = [P]
+        L.ns3d_ensemble_last_error.restype = ctypes.c_char_p
+        L.ns3d_ensemble_last_error.argtypes = [P]
+        L.ns3d_ensemble_initial_condition.restype = I
+        L.ns3d_ensemble_initial_condition.argtypes = [P, I, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_double,
+                                                      ctypes.c_double]
+        for n in ("ns3d_ensemble_set_state_host", "ns3d_ensemble_get_state_host"):
+            getattr(L, n).restype = I
+            getattr(L, n).argtypes = [P, I, D]
+        L.ns3d_ensemble_measurables.restype = I
+        L.ns3d_ensemble_measurables.argtypes = [P, I, ctypes.POINTER(Measures), D, D]
+        L.ns3d_ensemble_get_time.restype = I
+        L.ns3d_ensemble_get_time.argtypes = [P, I, D, D, ctypes.POINTER(ctypes.c_long)]
+        L.ns3d_ensemble_step.restype = I
+        L.ns3d_ensemble_step.argtypes = [P, I]
+        L.ns3d_ensemble_info.restype = I
+        L.ns3d_ensemble_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
+        L.ns3d_ensemble_last_step_ms.restype = I
+        L.ns3d_ensemble_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
         _lib = L
     return _lib
 
@@ -303,3 +329,80 @@ class Solver:
         cnt = ctypes.c_int()
         self._ck(lib().ns3d_profile_step(self._h, reps, names, ms, by, 16, ctypes.byref(cnt)))
         return [(names[i].decode(), ms[i], by[i]) for i in range(cnt.value)]
+
+
+def _params(N, nu=1.0, dt=1e-3, t0=0.0, visc_pow=1, integrator="ifrk4", precision="fp64", cfl=0.0,
+            forcing=None, force_k=2, device=0, stream=None):
+    integ = {"ifrk4": IFRK4, "rk4cn": RK4CN}[integrator.lower()]
+    prec = {"fp64": FP64, "fp32": FP32}[precision.lower()]
+    force = FORCE_SHELL if (forcing or "").upper() in ("SHELL", "ENERGY_SHELL") else FORCE_NONE
+    return Params(N, nu, dt, t0, visc_pow, integ, prec, cfl, force, force_k, device, stream)
+
+
+class Ensemble:
+    """Independent runs stepped together (ns3d_ensemble_*): one graph launch per
+    step advances every member; members of equal grid size share launches."""
+
+    def __init__(self, members):
+        """members: list of dicts with Solver keyword arguments (N, nu, dt, ...)."""
+        self.members = [dict(m) for m in members]
+        arr = (Params * len(members))(*[_params(**m) for m in members])
+        h = ctypes.c_void_p()
+        st = lib().ns3d_ensemble_create(arr, len(members), ctypes.byref(h))
+        if st != OK:
+            raise NS3DError(st, f"ns3d_ensemble_create: {lib().ns3d_status_string(st).decode()}")
+        self._h = h
+
+    def _ck(self, st):
+        if st != OK:
+            raise NS3DError(st, lib().ns3d_ensemble_last_error(self._h).decode() or
+                            lib().ns3d_status_string(st).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ns3d_ensemble_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def InitialConditions(self, member, name, seed=0, k0=4.0, energy=1.0):
+        self._ck(lib().ns3d_ensemble_initial_condition(self._h, member, name.encode(), seed, k0, energy))
+
+    def step(self, nsteps=1):
+        self._ck(lib().ns3d_ensemble_step(self._h, nsteps))
+
+    def get_state(self, member):
+        N = self.members[member]["N"]
+        out = np.empty((N, N, N // 2 + 1, 3), np.complex128)
+        self._ck(lib().ns3d_ensemble_get_state_host(self._h, member, _dp(out.view(np.float64))))
+        return out
+
+    def set_state(self, member, u_hat):
+        u = np.ascontiguousarray(u_hat, dtype=np.complex128)
+        self._ck(lib().ns3d_ensemble_set_state_host(self._h, member, _dp(u.view(np.float64))))
+
+    def measurables(self, member):
+        m = Measures()
+        ns = n_spect(self.members[member]["N"])
+        Ek, Ok = np.zeros(ns), np.zeros(ns)
+        self._ck(lib().ns3d_ensemble_measurables(self._h, member, ctypes.byref(m), _dp(Ek), _dp(Ok)))
+        return {k: getattr(m, k) for k, _ in Measures._fields_}, Ek, Ok
+
+    def get_time(self, member):
+        t, dt, it = ctypes.c_double(), ctypes.c_double(), ctypes.c_long()
+        self._ck(lib().ns3d_ensemble_get_time(self._h, member, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it)))
+        return t.value, dt.value, it.value
+
+    def info(self):
+        g, k = ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().ns3d_ensemble_info(self._h, ctypes.byref(g), ctypes.byref(k)))
+        return g.value, k.value
+
+    def last_step_ms(self):
+        v = ctypes.c_float()
+        self._ck(lib().ns3d_ensemble_last_step_ms(self._h, ctypes.byref(v)))
+        return v.value

@@ -52,6 +52,35 @@ void twiddle_table(int n, double* re, double* im) {
     }
 }
 
+// InitialConditions (solver.c:1537-1648) for the selected member of an engine,
+// with the if / else-if chain (D3 fixed).
+ns3d_status ic_dispatch(Base* impl, int N, const char* name, uint64_t seed, double k0, double energy) {
+    if (!strcmp(name, "TAYLOR_GREEN")) return impl->ic_real(0);
+    if (!strcmp(name, "SHAPIRO")) return impl->ic_real(1);
+    if (!strcmp(name, "TESTING")) return impl->ic_zero();
+    if (!strcmp(name, "SPECTRUM")) {
+        if (!(k0 > 0) || !(energy > 0)) {
+            impl->set_err("SPECTRUM needs k0 > 0 and energy > 0");
+            return NS3D_ERR_INVALID;
+        }
+        return impl->ic_spectrum(seed, k0, energy);
+    }
+    // RANDOM and unrecognised names: the reference's random modes
+    // (solver.c:1606-1625): srand(123456789), amplitude then phase per
+    // component, loop order i, j, k; dealiased on upload.
+    const int NF = N / 2 + 1;
+    std::vector<double> h((size_t)N * N * NF * 3 * 2);
+    srand(123456789);
+    for (size_t q = 0; q < (size_t)N * N * NF * 3; ++q) {
+        const double a = (double)rand() / (double)RAND_MAX;
+        const double ph = (double)rand() / (double)RAND_MAX;
+        const std::complex<double> v = a * std::exp(std::complex<double>(0.0, ph * 2.0 * M_PI));
+        h[2 * q] = v.real();
+        h[2 * q + 1] = v.imag();
+    }
+    return impl->ic_host(h.data());
+}
+
 }  // namespace ns3d
 
 struct ns3d_ctx {
@@ -124,7 +153,7 @@ ns3d_status ns3d_create(const ns3d_params* p, ns3d_ctx** out) {
         }
         c->own_stream = true;
     }
-    c->impl = p->precision == NS3D_FP32 ? ns3d::make_f32(p->N, *p, c->stream) : ns3d::make_f64(p->N, *p, c->stream);
+    c->impl = p->precision == NS3D_FP32 ? ns3d::make_f32(p->N, p, 1, c->stream) : ns3d::make_f64(p->N, p, 1, c->stream);
     if (!c->impl) {
         if (c->own_stream) cudaStreamDestroy(c->stream);
         free(c);
@@ -156,28 +185,7 @@ const char* ns3d_last_error(const ns3d_ctx* c) { return c ? c->err : "null conte
 
 ns3d_status ns3d_initial_condition(ns3d_ctx* c, const char* name, uint64_t seed, double k0, double energy) {
     if (!c || !name) return NS3D_ERR_INVALID;
-    // InitialConditions (solver.c:1537-1648) with the if / else-if chain (D3 fixed)
-    if (!strcmp(name, "TAYLOR_GREEN")) return pass(c, c->impl->ic_real(0));
-    if (!strcmp(name, "SHAPIRO")) return pass(c, c->impl->ic_real(1));
-    if (!strcmp(name, "TESTING")) return pass(c, c->impl->ic_zero());
-    if (!strcmp(name, "SPECTRUM")) {
-        if (!(k0 > 0) || !(energy > 0)) return fail(c, NS3D_ERR_INVALID, "SPECTRUM needs k0 > 0 and energy > 0");
-        return pass(c, c->impl->ic_spectrum(seed, k0, energy));
-    }
-    // RANDOM and unrecognised names: the reference's random modes
-    // (solver.c:1606-1625): srand(123456789), amplitude then phase per
-    // component, loop order i, j, k; dealiased on upload.
-    const int N = c->p.N, NF = N / 2 + 1;
-    std::vector<double> h((size_t)N * N * NF * 3 * 2);
-    srand(123456789);
-    for (size_t q = 0; q < (size_t)N * N * NF * 3; ++q) {
-        const double a = (double)rand() / (double)RAND_MAX;
-        const double ph = (double)rand() / (double)RAND_MAX;
-        const std::complex<double> v = a * std::exp(std::complex<double>(0.0, ph * 2.0 * M_PI));
-        h[2 * q] = v.real();
-        h[2 * q + 1] = v.imag();
-    }
-    return pass(c, c->impl->ic_host(h.data()));
+    return pass(c, ns3d::ic_dispatch(c->impl, c->p.N, name, seed, k0, energy));
 }
 
 ns3d_status ns3d_set_state_host(ns3d_ctx* c, const double* u) {

@@ -35,6 +35,13 @@ class Base {
     virtual ns3d_status get_forcing_target(double* e) = 0;
     virtual ns3d_status set_forcing_target(double e) = 0;
     virtual void* state_ptr() = 0;
+    // ensembles: number of members, selection of the member that single-run
+    // calls act on, enqueueing one step of every member on the engine's
+    // stream (for graph capture), and the health check of all members
+    virtual int members() const = 0;
+    virtual ns3d_status select(int m) = 0;
+    virtual void enqueue_step() = 0;
+    virtual ns3d_status status() = 0;
 
     const char* err() const { return err_; }
     void set_err(const char* fmt, ...) {
@@ -51,9 +58,10 @@ class Base {
     char err_[512];
 };
 
-// Factories, one per precision (ns3d_inst_f32.cu / ns3d_inst_f64.cu).
-Base* make_f32(int N, const ns3d_params& p, cudaStream_t s);
-Base* make_f64(int N, const ns3d_params& p, cudaStream_t s);
+// Factories, one per precision (ns3d_inst_f32.cu / ns3d_inst_f64.cu): an
+// engine for M members of grid size N with parameters ps[0..M-1].
+Base* make_f32(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f64(int N, const ns3d_params* ps, int M, cudaStream_t s);
 bool supported_n(int N);
 
 inline unsigned long long host_splitmix64(unsigned long long x) {

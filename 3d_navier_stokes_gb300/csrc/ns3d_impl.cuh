@@ -1,6 +1,12 @@
 // ns3d_impl.cuh — host-side engine for one (precision, grid size): device
 // memory plan, pass launches, CUDA-graph capture of a whole time step,
 // diagnostics, initial conditions and layout conversion.
+//
+// An engine holds M independent runs ("members") of the same grid size: every
+// per-run array is stored member after member, and each pass launch covers a
+// contiguous range of members (the member index is blockIdx.z, or part of the
+// z pass's work list). A single run is M = 1. Single-run operations (initial
+// conditions, diagnostics, host transfers, time) act on the selected member.
 #pragma once
 #include <cmath>
 #include <cstdio>
@@ -40,7 +46,24 @@ class Impl final : public Base {
     static constexpr int MWIDTH = 5 + 2 * G::NSP;
 
   public:
-    Impl(const ns3d_params& p, cudaStream_t s) : Base(p, s) {}
+    Impl(const ns3d_params* ps, int M, cudaStream_t s) : Base(ps[0], s), M_(M), mp_(ps, ps + M) {}
+
+    int members() const override { return M_; }
+    ns3d_status select(int m) override {
+        if (m < 0 || m >= M_) return NS3D_ERR_INVALID;
+        m_ = m;
+        return NS3D_OK;
+    }
+    void enqueue_step() override { launch_step(); }
+    ns3d_status status() override { return check_status(); }
+
+    // per-member views of the member-major arrays
+    cx<T>* Um(int m) const { return U_ + (size_t)m * 3 * G::FS; }
+    cx<T>* UTm(int m) const { return UT_ + (size_t)m * 3 * G::FS; }
+    cx<T>* ACCm(int m) const { return ACC_ + (size_t)m * 3 * G::FS; }
+    cx<T>* Wm(int m) const { return W_ + (size_t)m * 6 * G::FS; }
+    cx<T>* tabm(int m) const { return tab_ + (size_t)m * (G::KC2 + 1); }
+    StepDev* sdm(int m) const { return sd_ + m; }
 
     ~Impl() override {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
@@ -56,7 +79,7 @@ class Impl final : public Base {
     int kernels_per_step() const override { return 4 * 5 + (p_.cfl > 0 ? 1 : 0) + 1; }
 
     ns3d_status init() override {
-        const size_t fb = sizeof(cx<T>) * (size_t)G::FS;
+        const size_t fb = sizeof(cx<T>) * (size_t)G::FS * M_;
         NS3D_CK(cudaMalloc(&U_, 3 * fb));
         NS3D_CK(cudaMalloc(&UT_, 3 * fb));
         NS3D_CK(cudaMalloc(&ACC_, 3 * fb));
@@ -65,12 +88,12 @@ class Impl final : public Base {
         NS3D_CK(cudaMemsetAsync(UT_, 0, 3 * fb, s_));
         NS3D_CK(cudaMemsetAsync(ACC_, 0, 3 * fb, s_));
         NS3D_CK(cudaMalloc(&tw_, sizeof(cx<T>) * N));
-        NS3D_CK(cudaMalloc(&tab_, sizeof(cx<T>) * (G::KC2 + 1)));
+        NS3D_CK(cudaMalloc(&tab_, sizeof(cx<T>) * (G::KC2 + 1) * M_));
         NS3D_CK(cudaMalloc(&part_, sizeof(double) * NMEAS * MWIDTH));
         NS3D_CK(cudaMalloc(&mout_, sizeof(double) * MWIDTH));
         NS3D_CK(cudaMallocHost(&mout_host_, sizeof(double) * MWIDTH));
-        NS3D_CK(cudaMalloc(&sd_, sizeof(StepDev)));
-        NS3D_CK(cudaMallocHost(&sd_host_, sizeof(StepDev)));
+        NS3D_CK(cudaMalloc(&sd_, sizeof(StepDev) * M_));
+        NS3D_CK(cudaMallocHost(&sd_host_, sizeof(StepDev) * M_));
         NS3D_CK(cudaEventCreate(&ev0_));
         NS3D_CK(cudaEventCreate(&ev1_));
         // twiddles
@@ -80,10 +103,12 @@ class Impl final : public Base {
         for (int m = 0; m < N; ++m) { h[m].x = T(re[m]); h[m].y = T(im[m]); }
         NS3D_CK(cudaMemcpyAsync(tw_, h.data(), sizeof(cx<T>) * N, cudaMemcpyHostToDevice, s_));
         // step state
-        StepDev sd{};
-        sd.t = p_.t0; sd.dt = p_.dt; sd.t0 = p_.t0; sd.nu = p_.nu; sd.cfl = p_.cfl;
-        *sd_host_ = sd;
-        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        for (int m = 0; m < M_; ++m) {
+            StepDev sd{};
+            sd.t = mp_[m].t0; sd.dt = mp_[m].dt; sd.t0 = mp_[m].t0; sd.nu = mp_[m].nu; sd.cfl = mp_[m].cfl;
+            sd_host_[m] = sd;
+        }
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
         // opt-in shared memory sizes
         NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
@@ -101,8 +126,8 @@ class Impl final : public Base {
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
-        ns3d_status st = refresh_tables();
-        if (st != NS3D_OK) return st;
+        tables(0, 0, M_);
+        NS3D_CK(cudaGetLastError());
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
@@ -124,49 +149,56 @@ class Impl final : public Base {
         cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
     }
 
-    void p1(const cx<T>* in) {
-        k_xinv<T, N><<<dim3(NTX, G::NKY), TX * PX::P, smem_x(), s_>>>(in, W_, tw_);
+    // each launcher covers members [m0, m0 + cnt); `in` points at member 0's arrays
+    void p1(const cx<T>* in, int m0, int cnt) {
+        k_xinv<T, N><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
     }
-    void p2() { k_ypass<T, N, true><<<dim3(NTA, N, 6), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
+    void p2(int m0, int cnt) {
+        k_ypass<T, N, true><<<dim3(NTA, N, 6 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+    }
     static constexpr size_t smem_zl() { return zline_smem<T, N>(); }
-    void p3(int want_umax) {
+    void p3(int want_umax, int m0, int cnt) {
         if constexpr (zline_ok<T, N>()) {
             // persistent: as many CTAs as fit on the device, never more than there are warp tasks
-            const long long groups = (long long)N * N / zline_gpw<N>();
+            const long long groups = (long long)N * N / zline_gpw<N>() * cnt;
             long long grid = (long long)zline_ctas_;
             if (grid * ZLINE_WARPS > groups) grid = (groups + ZLINE_WARPS - 1) / ZLINE_WARPS;
-            k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(W_, tw_, sd_, want_umax);
+            k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(Wm(m0), tw_, sdm(m0), want_umax, cnt);
         } else {
-            k_zpass<T, N, 0><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
-                W_, tw_, nullptr, &sd_->umax_bits, want_umax);
+            k_zpass<T, N, 0><<<dim3((unsigned)((long long)N * N / 2 / ZP), cnt), 3 * PA::P * ZP, smem_z(), s_>>>(
+                Wm(m0), tw_, nullptr, sdm(m0), want_umax);
         }
     }
-    void p4() { k_ypass<T, N, false><<<dim3(NTA, N, 3), TA * PA::P, smem_a(), s_>>>(W_, tw_); }
+    void p4(int m0, int cnt) {
+        k_ypass<T, N, false><<<dim3(NTA, N, 3 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+    }
     template <int INTEG, int MODE>
-    void p5x(cx<T>* out) {
-        k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY), TX * PX::P, smem_x(), s_>>>(
-            W_, U_, UT_, out ? out : ACC_, tw_, sd_, tab_);
+    void p5x(int m0, int cnt, cx<T>* out) {
+        k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+            Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0));
     }
     template <int MODE>
-    void p5(cx<T>* out = nullptr) {
-        if (p_.integrator == INT_RK4CN) p5x<INT_RK4CN, MODE>(out);
-        else p5x<INT_IFRK4, MODE>(out);
+    void p5(int m0, int cnt, cx<T>* out = nullptr) {
+        if (p_.integrator == INT_RK4CN) p5x<INT_RK4CN, MODE>(m0, cnt, out);
+        else p5x<INT_IFRK4, MODE>(m0, cnt, out);
     }
-    void tables(int use_cfl) {
+    void tables(int use_cfl, int m0, int cnt) {
         const int n = G::KC2 + 1;
-        k_tables<T, N><<<(n + 255) / 256, 256, 0, s_>>>(tab_, sd_, p_.integrator, p_.visc_pow, use_cfl);
+        k_tables<T, N><<<dim3((n + 255) / 256, cnt), 256, 0, s_>>>(tabm(m0), sdm(m0), p_.integrator, p_.visc_pow,
+                                                                   use_cfl);
     }
 
-    // one time step = 4 nonlinear evaluations with fused stage epilogues
+    // one time step of every member = 4 nonlinear evaluations with fused stage epilogues
     void launch_step() {
         const int cfl = p_.cfl > 0 ? 1 : 0;
-        p1(U_); p2(); p3(cfl);
-        if (cfl) tables(1);
-        p4(); p5<X_STAGE1>();
-        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE2>();
-        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE3>();
-        p1(UT_); p2(); p3(0); p4(); p5<X_STAGE4>();
-        k_step_end<T, N><<<1, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+        const int M = M_;
+        p1(U_, 0, M); p2(0, M); p3(cfl, 0, M);
+        if (cfl) tables(1, 0, M);
+        p4(0, M); p5<X_STAGE1>(0, M);
+        p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE2>(0, M);
+        p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE3>(0, M);
+        p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE4>(0, M);
+        k_step_end<T, N><<<M, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
     }
 
     ns3d_status build_graph() {
@@ -200,16 +232,19 @@ class Impl final : public Base {
     }
 
     ns3d_status check_status() {
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev) * M_, cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         NS3D_CK(cudaGetLastError());
-        if (sd_host_->status == kStatusTimeout) {
-            set_err("a bounded wait for an asynchronous copy gave up at step %lld", sd_host_->iters);
-            return NS3D_ERR_TIMEOUT;
-        }
-        if (sd_host_->status != 0) {
-            set_err("numeric health check failed at step %lld (NaN/Inf energy or speed)", sd_host_->iters);
-            return NS3D_ERR_NUMERIC;
+        for (int m = 0; m < M_; ++m) {
+            if (sd_host_[m].status == kStatusTimeout) {
+                set_err("member %d: a bounded wait for an asynchronous copy gave up at step %lld", m, sd_host_[m].iters);
+                return NS3D_ERR_TIMEOUT;
+            }
+            if (sd_host_[m].status != 0) {
+                set_err("member %d: numeric health check failed at step %lld (NaN/Inf energy or speed)", m,
+                        sd_host_[m].iters);
+                return NS3D_ERR_NUMERIC;
+            }
         }
         return NS3D_OK;
     }
@@ -230,16 +265,18 @@ class Impl final : public Base {
             int q = 0;
             for (int s = 0; s < 4; ++s) {
                 const cx<T>* in = s == 0 ? U_ : UT_;
-                NS3D_CK(cudaEventRecord(ev[q++], s_)); p1(in);
-                NS3D_CK(cudaEventRecord(ev[q++], s_)); p2();
-                NS3D_CK(cudaEventRecord(ev[q++], s_)); p3(s == 0 ? cfl : 0);
-                if (s == 0 && cfl) tables(1);
-                NS3D_CK(cudaEventRecord(ev[q++], s_)); p4();
+                const int M = M_;
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p1(in, 0, M);
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p2(0, M);
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p3(s == 0 ? cfl : 0, 0, M);
+                if (s == 0 && cfl) tables(1, 0, M);
+                NS3D_CK(cudaEventRecord(ev[q++], s_)); p4(0, M);
                 NS3D_CK(cudaEventRecord(ev[q++], s_));
-                if (s == 0) p5<X_STAGE1>(); else if (s == 1) p5<X_STAGE2>(); else if (s == 2) p5<X_STAGE3>(); else p5<X_STAGE4>();
+                if (s == 0) p5<X_STAGE1>(0, M); else if (s == 1) p5<X_STAGE2>(0, M);
+                else if (s == 2) p5<X_STAGE3>(0, M); else p5<X_STAGE4>(0, M);
                 NS3D_CK(cudaEventRecord(ev[q++], s_));
             }
-            k_step_end<T, N><<<1, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+            k_step_end<T, N><<<M_, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
             NS3D_CK(cudaEventRecord(ev[q++], s_));
             NS3D_CK(cudaStreamSynchronize(s_));
             q = 0;
@@ -292,10 +329,10 @@ class Impl final : public Base {
 
     // --------------------------------------------------------------- rhs
     ns3d_status rhs_host(const double* in, double* out) override {
-        ns3d_status st = upload(in, UT_);
+        ns3d_status st = upload(in, UTm(m_));
         if (st != NS3D_OK) return st;
-        p1(UT_); p2(); p3(0); p4(); p5<X_RHS>(ACC_);
-        return download(ACC_, out);
+        p1(UT_, m_, 1); p2(m_, 1); p3(0, m_, 1); p4(m_, 1); p5<X_RHS>(m_, 1, ACC_);
+        return download(ACCm(m_), out);
     }
 
     // ----------------------------------------------------- state transfer
@@ -329,14 +366,15 @@ class Impl final : public Base {
     }
 
     ns3d_status set_state_host(const double* u) override {
-        ns3d_status st = upload(u, U_);
+        ns3d_status st = upload(u, Um(m_));
         if (st != NS3D_OK) return st;
         return reset_forcing_target();
     }
-    ns3d_status get_state_host(double* u) override { return download(U_, u); }
+    ns3d_status get_state_host(double* u) override { return download(Um(m_), u); }
 
     ns3d_status step_host(const double* in, double* out) override {
         ns3d_status st;
+        if (M_ != 1) return NS3D_ERR_INVALID;
         if (in && (st = upload(in, U_)) != NS3D_OK) return st;
         if ((st = build_graph()) != NS3D_OK) return st;
         NS3D_CK(cudaGraphLaunch(graph_exec_, s_));
@@ -348,7 +386,7 @@ class Impl final : public Base {
 
     // -------------------------------------------------------- diagnostics
     ns3d_status measure_dev(const cx<T>* u) {
-        k_measure<T, N><<<(unsigned)NMEAS, MEAS_WARPS * 32, 0, s_>>>(u, p_.nu, p_.visc_pow, part_);
+        k_measure<T, N><<<(unsigned)NMEAS, MEAS_WARPS * 32, 0, s_>>>(u, mp_[m_].nu, p_.visc_pow, part_);
         const double N3 = (double)N * N * N;
         k_measure_reduce<<<(MWIDTH + 127) / 128, 128, 0, s_>>>(part_, (int)NMEAS, MWIDTH, G::NSP, N3 * N3, mout_);
         NS3D_CK(cudaMemcpyAsync(mout_host_, mout_, sizeof(double) * MWIDTH, cudaMemcpyDeviceToHost, s_));
@@ -357,7 +395,7 @@ class Impl final : public Base {
         return NS3D_OK;
     }
     ns3d_status measurables(ns3d_measures* m, double* Ek, double* Ok) override {
-        ns3d_status st = measure_dev(U_);
+        ns3d_status st = measure_dev(Um(m_));
         if (st != NS3D_OK) return st;
         if (m) {
             m->energy = mout_host_[0];
@@ -385,34 +423,34 @@ class Impl final : public Base {
         if (st != NS3D_OK) return st;
         k_fill_real<T, N><<<grid_for((long long)N * N * N), 256, 0, s_>>>(real_, kind);
         k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
-            W_, tw_, real_, nullptr, 0);
-        p4();
-        p5<X_PLAIN>(U_);
+            Wm(m_), tw_, real_, nullptr, 0);
+        p4(m_, 1);
+        p5<X_PLAIN>(m_, 1, U_);
         NS3D_CK(cudaGetLastError());
         return finish_ic();
     }
     ns3d_status ic_spectrum(uint64_t seed, double k0, double energy) override {
         unsigned long long key = host_splitmix64(seed);
-        k_spectrum_ic<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(U_, key, k0);
-        ns3d_status st = measure_dev(U_);
+        k_spectrum_ic<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(Um(m_), key, k0);
+        ns3d_status st = measure_dev(Um(m_));
         if (st != NS3D_OK) return st;
         const double e = mout_host_[0];
         const double target = 8.0 * M_PI * M_PI * M_PI * energy;
-        if (e > 0.0) k_scale<T, N><<<grid_for(3 * G::FS), 256, 0, s_>>>(U_, std::sqrt(target / e));
+        if (e > 0.0) k_scale<T, N><<<grid_for(3 * G::FS), 256, 0, s_>>>(Um(m_), std::sqrt(target / e));
         NS3D_CK(cudaGetLastError());
         return finish_ic();
     }
     ns3d_status ic_host(const double* u) override {
-        ns3d_status st = upload(u, U_);
+        ns3d_status st = upload(u, Um(m_));
         if (st != NS3D_OK) return st;
         return finish_ic();
     }
     ns3d_status ic_zero() override {
-        NS3D_CK(cudaMemsetAsync(U_, 0, sizeof(cx<T>) * 3 * (size_t)G::FS, s_));
+        NS3D_CK(cudaMemsetAsync(Um(m_), 0, sizeof(cx<T>) * 3 * (size_t)G::FS, s_));
         return finish_ic();
     }
     ns3d_status finish_ic() {
-        ns3d_status st = set_time(p_.t0, p_.dt, 0);
+        ns3d_status st = set_time(mp_[m_].t0, mp_[m_].dt, 0);
         if (st != NS3D_OK) return st;
         return reset_forcing_target();
     }
@@ -425,7 +463,7 @@ class Impl final : public Base {
     }
     // energy of shells 1 <= round(|k|) <= force_k, FP64, from the spectrum
     ns3d_status shell_energy(double* e) {
-        ns3d_status st = measure_dev(U_);
+        ns3d_status st = measure_dev(Um(m_));
         if (st != NS3D_OK) return st;
         double s = 0;
         for (int b = 1; b <= p_.force_k && b < G::NSP; ++b) s += mout_host_[5 + b];
@@ -440,9 +478,9 @@ class Impl final : public Base {
         double* du = nullptr;
         size_t rb = sizeof(double) * 3 * (size_t)N * N * (N + 2);
         NS3D_CK(cudaMalloc(&du, 2 * rb));
-        p1(U_); p2();
+        p1(U_, m_, 1); p2(m_, 1);
         k_zpass<T, N, 1><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
-            W_, tw_, real_, nullptr, 0);
+            Wm(m_), tw_, real_, nullptr, 0);
         k_real_unpack<T, N><<<grid_for((long long)N * N * (N + 2)), 256, 0, s_>>>(real_, du, du + rb / sizeof(double));
         cudaError_t e = cudaGetLastError();
         if (e == cudaSuccess && u) e = cudaMemcpyAsync(u, du, rb, cudaMemcpyDeviceToHost, s_);
@@ -457,9 +495,9 @@ class Impl final : public Base {
     }
 
     ns3d_status max_speed_sum(double* umax) override {
-        NS3D_CK(cudaMemsetAsync(&sd_->umax_bits, 0, sizeof(unsigned long long), s_));
-        p1(U_); p2(); p3(1);
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemsetAsync(&sdm(m_)->umax_bits, 0, sizeof(unsigned long long), s_));
+        p1(U_, m_, 1); p2(m_, 1); p3(1, m_, 1);
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         const unsigned long long b = sd_host_->umax_bits;
         if (sizeof(T) == 4) {
@@ -472,19 +510,19 @@ class Impl final : public Base {
             std::memcpy(&d, &b, 8);
             *umax = d;
         }
-        NS3D_CK(cudaMemsetAsync(&sd_->umax_bits, 0, sizeof(unsigned long long), s_));
+        NS3D_CK(cudaMemsetAsync(&sdm(m_)->umax_bits, 0, sizeof(unsigned long long), s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
 
     // ------------------------------------------------------ bookkeeping
     ns3d_status refresh_tables() {
-        tables(0);
+        tables(0, m_, 1);
         NS3D_CK(cudaGetLastError());
         return NS3D_OK;
     }
     ns3d_status get_time(double* t, double* dt, long* iters) override {
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         if (t) *t = sd_host_->t;
         if (dt) *dt = sd_host_->dt;
@@ -492,7 +530,7 @@ class Impl final : public Base {
         return NS3D_OK;
     }
     ns3d_status set_time(double t, double dt, long iters) override {
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         sd_host_->t = t;
         sd_host_->dt = dt;
@@ -500,29 +538,29 @@ class Impl final : public Base {
         sd_host_->t0 = t - (p_.cfl > 0 ? 0.0 : (double)iters * dt);
         sd_host_->umax_bits = 0;
         sd_host_->status = 0;
-        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaMemcpyAsync(sdm(m_), sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
         ns3d_status st = refresh_tables();
         if (st != NS3D_OK) return st;
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
     ns3d_status get_forcing_target(double* e) override {
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         *e = sd_host_->force_target;
         return NS3D_OK;
     }
     ns3d_status set_forcing_target(double e) override {
-        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         sd_host_->force_target = e;
-        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaMemcpyAsync(sdm(m_), sd_host_, sizeof(StepDev), cudaMemcpyHostToDevice, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
 
     // device pointers for in-library tools
-    void* state_ptr() override { return U_; }
+    void* state_ptr() override { return Um(m_); }
 
   private:
     cx<T>* U_ = nullptr;
@@ -541,6 +579,9 @@ class Impl final : public Base {
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     int zline_ctas_ = 1;
+    int M_ = 1;                    // members
+    int m_ = 0;                    // selected member
+    std::vector<ns3d_params> mp_;  // per-member parameters
 };
 
 }  // namespace ns3d

@@ -8,11 +8,11 @@
 
 namespace ns3d {
 template <typename T>
-Base* make_typed(int N, const ns3d_params& p, cudaStream_t s) {
+Base* make_typed(int N, const ns3d_params* ps, int M, cudaStream_t s) {
     switch (N) {
 #define NS3D_CASE(n) \
     case n:          \
-        return new Impl<T, n>(p, s);
+        return new Impl<T, n>(ps, M, s);
         NS3D_SIZES(NS3D_CASE)
 #undef NS3D_CASE
         default:

@@ -3,5 +3,7 @@
 #include "ns3d_inst.cuh"
 
 namespace ns3d {
-Base* make_f32(int N, const ns3d_params& p, cudaStream_t s) { return make_typed<float>(N, p, s); }
+Base* make_f32(int N, const ns3d_params* ps, int M, cudaStream_t s) {
+    return make_typed<float>(N, ps, M, s);
+}
 }  // namespace ns3d

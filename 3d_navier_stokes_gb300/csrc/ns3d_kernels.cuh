@@ -131,6 +131,9 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     const int kz = blockIdx.x * TT + t;
     const int ky = (int)blockIdx.y - G::KC;
     const int j = ky < 0 ? ky + N : ky;
+    // ensemble member (blockIdx.z): its arrays follow the previous member's
+    U += (long long)blockIdx.z * 3 * G::FS;
+    W += (long long)blockIdx.z * 6 * G::FS;
     // whole CTA idle when every column of the tile is outside the circle
     const int kz0 = blockIdx.x * TT;
     if (ky * ky + kz0 * kz0 > G::KC2) return;
@@ -207,7 +210,10 @@ k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     const int kz = blockIdx.x * TT + t;
     const bool colok = kz <= G::KC;
     const int rem = G::KC2 - kz * kz;
-    cx<T>* base = W + (long long)blockIdx.z * G::FS + (long long)blockIdx.y * N * G::NZP + kz;
+    // blockIdx.z = member * (fields per member) + field: 6 fields inverse, the first 3 forward
+    constexpr int NF = INV ? 6 : 3;
+    const long long fld = (long long)(blockIdx.z / NF) * 6 + blockIdx.z % NF;
+    cx<T>* base = W + fld * G::FS + (long long)blockIdx.y * N * G::NZP + kz;
     StridedIdx<TT> sidx{t};
     SyncBlock sync;
     cx<T> v[E];
@@ -256,11 +262,14 @@ template <int N> constexpr int zpad() { return N + (N >> 4); }
 template <typename T, int N, int MODE>
 __global__ void __launch_bounds__(3 * Plans<N>::A::P * zpairs<N>())
 k_zpass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, T* __restrict__ real,
-        unsigned long long* __restrict__ umax_bits, int want_umax) {
+        StepDev* __restrict__ sd, int want_umax) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
     constexpr int E = PL::E, P = PL::P, ZP = zpairs<N>();
     constexpr int XS = zpad<N>();
+    // ensemble member (blockIdx.y); the real-space modes handle one member only
+    W += (long long)blockIdx.y * 6 * G::FS;
+    unsigned long long* umax_bits = sd ? &sd[blockIdx.y].umax_bits : nullptr;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* xbuf = reinterpret_cast<cx<T>*>(smem_raw);                       // [ZP][3][XS]
     T* R = reinterpret_cast<T*>(smem_raw + sizeof(cx<T>) * ZP * 3 * XS);     // [ZP][2][6][N]
@@ -421,12 +430,13 @@ template <typename T, int N> constexpr size_t zline_smem() {
 
 template <typename T, int N>
 __global__ void __launch_bounds__(ZLINE_WARPS * 32)
-k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, int want_umax) {
+k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, int want_umax,
+        int nmem) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
     constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>();
     constexpr int NZP = G::NZP;
-    constexpr long long NG = (long long)N * N / GPW;   // line groups
+    constexpr long long NG = (long long)N * N / GPW;   // line groups per ensemble member
     constexpr int SE = GPW * 6 * NZP;                  // elements per stage
     constexpr uint32_t STAGE_BYTES = SE * sizeof(cx<T>);
     constexpr uint32_t LINE_BYTES = NZP * sizeof(cx<T>);
@@ -451,32 +461,49 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         if (lane == 0) {
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bars[s], STAGE_BYTES);
+            const long long m = g / NG, gl = g % NG;
             for (int l = 0; l < GPW; ++l)
                 for (int f = 0; f < 6; ++f)
-                    bulk_g2s(stage[s] + (l * 6 + f) * NZP, W + (long long)f * G::FS + (g * GPW + l) * NZP,
+                    bulk_g2s(stage[s] + (l * 6 + f) * NZP, W + (m * 6 + f) * G::FS + (gl * GPW + l) * NZP,
                              LINE_BYTES, &bars[s]);
         }
     };
 
     const long long nw = (long long)gridDim.x * ZLINE_WARPS;
     long long g = (long long)blockIdx.x * ZLINE_WARPS + warp;
-    uint32_t phase = 0;   // bit s = parity to wait for on stage s
+    const long long NGT = NG * nmem;   // work items over all members
+    uint32_t phase = 0;                // bit s = parity to wait for on stage s
     T um = T(0);
+    long long cur = -1;                // member whose speed bound um holds
+    auto flush_umax = [&]() {
+        if (want_umax && cur >= 0) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) um = fmaxf(um, __shfl_xor_sync(0xffffffffu, um, o));
+            if (lane == 0) Bits<T>::amax(&sd[cur].umax_bits, um);
+        }
+        um = T(0);
+    };
     int s = 0;
-    if (g < NG) issue(g, 0);
-    for (; g < NG; g += nw, s ^= 1) {
-        const bool more = g + nw < NG;
+    if (g < NGT) issue(g, 0);
+    for (; g < NGT; g += nw, s ^= 1) {
+        const bool more = g + nw < NGT;
         if (more) issue(g + nw, s ^ 1);
         const bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], (phase >> s) & 1u));
         phase ^= 1u << s;
         if (!ok) {
             // record the timeout, let the copy already issued for the next group land, leave
             if (more) (void)mbar_wait(&bars[s ^ 1], (phase >> (s ^ 1)) & 1u);
-            if (lane == 0) atomicExch(&sd->status, kStatusTimeout);
+            if (lane == 0) atomicExch(&sd[g / NG].status, kStatusTimeout);
             return;
         }
+        const long long mem = g / NG;
+        if (mem != cur) {
+            flush_umax();
+            cur = mem;
+        }
+        cx<T>* Wm = W + mem * 6 * G::FS;
         const cx<T>* in = stage[s] + gi * 6 * NZP;
-        const long long line = g * GPW + gi;
+        const long long line = (g % NG) * GPW + gi;
 
         auto load_pair = [&](int f, cx<T>(&v)[E]) {
             const cx<T>* A = in + f * NZP;
@@ -519,7 +546,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         for (int q = 0; q < E; ++q) sb[sidx(p + P * q)] = V1[q];
         __syncwarp();
         {
-            cx<T>* outA = W + line * NZP;
+            cx<T>* outA = Wm + line * NZP;
             cx<T>* outB = outA + G::FS;
             const T half = T(0.5);
 #pragma unroll
@@ -537,7 +564,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         __syncwarp();
         // Nz (real input): its spectrum is the transform itself
         PL::fwd(V2, sb, p, tw, sidx, sync);
-        cx<T>* outC = W + 2 * G::FS + line * NZP;
+        cx<T>* outC = Wm + 2 * G::FS + line * NZP;
 #pragma unroll
         for (int q = 0; q < E; ++q) {
             const int m = p + P * q;
@@ -545,11 +572,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         }
         __syncwarp();
     }
-    if (want_umax) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) um = fmaxf(um, __shfl_xor_sync(0xffffffffu, um, o));
-        if (lane == 0) Bits<T>::amax(&sd->umax_bits, um);
-    }
+    flush_umax();
 }
 // ---------------------------------------------------------------------------
 // P5: forward FFT along x of the 3 product fields, then per mode the Leray
@@ -572,6 +595,16 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     const int kz = blockIdx.x * TT + t;
     const int ky = (int)blockIdx.y - G::KC;
     const int j = ky < 0 ? ky + N : ky;
+    // ensemble member (blockIdx.z)
+    {
+        const long long mem = blockIdx.z;
+        W += mem * 6 * G::FS;
+        U += mem * 3 * G::FS;
+        UT += mem * 3 * G::FS;
+        ACC += mem * 3 * G::FS;
+        sd += mem;
+        tab += mem * (G::KC2 + 1);
+    }
     const int kz0 = blockIdx.x * TT;
     if (ky * ky + kz0 * kz0 > G::KC2) return;
     const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
@@ -671,6 +704,8 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
 template <typename T, int N>
 __global__ void k_tables(cx<T>* __restrict__ tab, StepDev* __restrict__ sd, int integ, int vp, int use_cfl) {
     using G = Geo<N>;
+    sd += blockIdx.y;   // ensemble member
+    tab += (long long)blockIdx.y * (G::KC2 + 1);
     double h = sd->dt;
     if (use_cfl) {
         const unsigned long long b = sd->umax_bits;
@@ -707,6 +742,8 @@ __global__ void k_tables(cx<T>* __restrict__ tab, StepDev* __restrict__ sd, int 
 template <typename T, int N>
 __global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int force_k, int use_cfl) {
     using G = Geo<N>;
+    U += (long long)blockIdx.x * 3 * G::FS;   // one CTA per ensemble member
+    sd += blockIdx.x;
     __shared__ double red[256];
     const int kb = force_k;
     const int side = 2 * kb + 1;

@@ -145,6 +145,30 @@ ns3d_status ns3d_set_forcing_target(ns3d_ctx* ctx, double e);
 /* Largest |u|+|v|+|w| over the grid for the current state (CFL numerator). */
 ns3d_status ns3d_max_speed_sum(ns3d_ctx* ctx, double* umax);
 
+/* ------------------------------------------------------------------------
+ * Ensembles: many independent runs of (possibly) different grid sizes,
+ * viscosities, time steps and initial conditions stepped together. Members
+ * with the same N, precision, integrator, visc_pow, forcing and CFL switch
+ * share kernel launches; all members advance by one step per CUDA-graph
+ * launch. Member operations mirror the single-run calls above.
+ * ------------------------------------------------------------------------ */
+typedef struct ns3d_ensemble ns3d_ensemble;
+ns3d_status ns3d_ensemble_create(const ns3d_params* members, int count, ns3d_ensemble** out);
+ns3d_status ns3d_ensemble_destroy(ns3d_ensemble* e);
+const char* ns3d_ensemble_last_error(const ns3d_ensemble* e);
+ns3d_status ns3d_ensemble_initial_condition(ns3d_ensemble* e, int member, const char* name, uint64_t seed,
+                                            double k0, double energy);
+ns3d_status ns3d_ensemble_set_state_host(ns3d_ensemble* e, int member, const double* u_hat);
+ns3d_status ns3d_ensemble_get_state_host(ns3d_ensemble* e, int member, double* u_hat);
+ns3d_status ns3d_ensemble_measurables(ns3d_ensemble* e, int member, ns3d_measures* out, double* Ek, double* Ok);
+ns3d_status ns3d_ensemble_get_time(ns3d_ensemble* e, int member, double* t, double* dt, long* iters);
+/* every member advances nsteps steps (one graph launch per step) */
+ns3d_status ns3d_ensemble_step(ns3d_ensemble* e, int nsteps);
+/* number of launch groups and kernels launched per ensemble step */
+ns3d_status ns3d_ensemble_info(ns3d_ensemble* e, int* groups, int* kernels_per_step);
+/* device time of the last ns3d_ensemble_step call, milliseconds */
+ns3d_status ns3d_ensemble_last_step_ms(ns3d_ensemble* e, float* ms);
+
 /* Instrumentation for benchmarks: the stream the context runs on, the number
  * of kernels one step launches, and the device time of the last ns3d_step
  * call (CUDA events on the context stream), in milliseconds. */
