@@ -40,7 +40,11 @@ EXPORTS = (
     "ns3d_ensemble_create", "ns3d_ensemble_destroy", "ns3d_ensemble_last_error",
     "ns3d_ensemble_initial_condition", "ns3d_ensemble_set_state_host", "ns3d_ensemble_get_state_host",
     "ns3d_ensemble_measurables", "ns3d_ensemble_get_time", "ns3d_ensemble_step", "ns3d_ensemble_info",
-    "ns3d_ensemble_last_step_ms",
+    "ns3d_ensemble_last_step_ms", "ns3d_set_state_real_host",
+    "ns3d_les_num_params", "ns3d_les_create", "ns3d_les_destroy", "ns3d_les_last_error", "ns3d_les_add_snapshot",
+    "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
+    "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
+    "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters",
 )
 
 
@@ -162,6 +166,41 @@ def lib():
         L.ns3d_ensemble_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
         L.ns3d_ensemble_last_step_ms.restype = I
         L.ns3d_ensemble_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
+        F = ctypes.POINTER(ctypes.c_float)
+        L.ns3d_set_state_real_host.restype = I
+        L.ns3d_set_state_real_host.argtypes = [P, D]
+        L.ns3d_les_num_params.restype = I
+        L.ns3d_les_num_params.argtypes = []
+        L.ns3d_les_create.restype = I
+        L.ns3d_les_create.argtypes = [I, I, ctypes.c_uint64, ctypes.POINTER(P)]
+        L.ns3d_les_destroy.restype = I
+        L.ns3d_les_destroy.argtypes = [P]
+        L.ns3d_les_last_error.restype = ctypes.c_char_p
+        L.ns3d_les_last_error.argtypes = [P]
+        L.ns3d_les_add_snapshot.restype = I
+        L.ns3d_les_add_snapshot.argtypes = [P, P]
+        L.ns3d_les_dataset_size.restype = I
+        L.ns3d_les_dataset_size.argtypes = [P, ctypes.POINTER(I)]
+        L.ns3d_les_filtered_velocity_host.restype = I
+        L.ns3d_les_filtered_velocity_host.argtypes = [P, P, D]
+        L.ns3d_les_set_scales.restype = I
+        L.ns3d_les_set_scales.argtypes = [P, ctypes.c_double, ctypes.c_double]
+        L.ns3d_les_get_scales.restype = I
+        L.ns3d_les_get_scales.argtypes = [P, D, D]
+        L.ns3d_les_train.restype = I
+        L.ns3d_les_train.argtypes = [P, I, ctypes.c_double, D]
+        L.ns3d_les_dataset_loss.restype = I
+        L.ns3d_les_dataset_loss.argtypes = [P, D]
+        L.ns3d_les_weights_host.restype = I
+        L.ns3d_les_weights_host.argtypes = [P, F, I]
+        L.ns3d_les_gradients_host.restype = I
+        L.ns3d_les_gradients_host.argtypes = [P, F, F, D, F]
+        L.ns3d_les_forward_host.restype = I
+        L.ns3d_les_forward_host.argtypes = [P, F, F]
+        L.ns3d_les_attach.restype = I
+        L.ns3d_les_attach.argtypes = [P, P]
+        L.ns3d_les_counters.restype = I
+        L.ns3d_les_counters.argtypes = [P, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_long)]
         _lib = L
     return _lib
 
@@ -290,6 +329,19 @@ class Solver:
         self._ck(lib().ns3d_get_time(self._h, ctypes.byref(t), ctypes.byref(dt), ctypes.byref(it)))
         return t.value, dt.value, it.value
 
+    def set_state_real(self, u: np.ndarray):
+        """r2c + dealiasing of a real-space velocity in the reference layout [N][N][N+2][3]."""
+        a = np.ascontiguousarray(u, dtype=np.float64).reshape(self.rshape)
+        self._ck(lib().ns3d_set_state_real_host(self._h, _dp(a)))
+
+    def attach_closure(self, les: "LES | None"):
+        self._ck(lib().ns3d_les_attach(self._h, les._h if les is not None else None))
+
+    def closure_counters(self):
+        a, b = ctypes.c_long(), ctypes.c_long()
+        self._ck(lib().ns3d_les_counters(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
     def set_time(self, t: float, dt: float, iters: int):
         self._ck(lib().ns3d_set_time(self._h, t, dt, iters))
 
@@ -406,3 +458,97 @@ class Ensemble:
         v = ctypes.c_float()
         self._ck(lib().ns3d_ensemble_last_step_ms(self._h, ctypes.byref(v)))
         return v.value
+
+
+
+def _fp(a: np.ndarray):
+    assert a.dtype == np.float32 and a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class LES:
+    """Learned subgrid closure (ns3d_les_*): dataset of box-filtered fine-run
+    snapshots, a 3D CNN trained on the GPU, attachable to a coarse run."""
+
+    def __init__(self, Nc: int, capacity: int = 0, seed: int = 0):
+        self.Nc = Nc
+        h = ctypes.c_void_p()
+        st = lib().ns3d_les_create(Nc, capacity, seed, ctypes.byref(h))
+        if st != OK:
+            raise NS3DError(st, f"ns3d_les_create: {lib().ns3d_status_string(st).decode()}")
+        self._h = h
+
+    def _ck(self, st):
+        if st != OK:
+            raise NS3DError(st, lib().ns3d_les_last_error(self._h).decode() or lib().ns3d_status_string(st).decode())
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().ns3d_les_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def num_params() -> int:
+        return lib().ns3d_les_num_params()
+
+    def add_snapshot(self, fine: Solver):
+        self._ck(lib().ns3d_les_add_snapshot(self._h, fine._h))
+
+    @property
+    def size(self) -> int:
+        n = ctypes.c_int()
+        self._ck(lib().ns3d_les_dataset_size(self._h, ctypes.byref(n)))
+        return n.value
+
+    def filtered_velocity(self, fine: Solver) -> np.ndarray:
+        N = self.Nc
+        out = np.empty((N, N, N + 2, 3), np.float64)
+        self._ck(lib().ns3d_les_filtered_velocity_host(self._h, fine._h, _dp(out)))
+        return out
+
+    def set_scales(self, s_in: float, s_out: float):
+        self._ck(lib().ns3d_les_set_scales(self._h, s_in, s_out))
+
+    def scales(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._ck(lib().ns3d_les_get_scales(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
+
+    def train(self, iterations: int, lr: float = 1e-3) -> float:
+        v = ctypes.c_double()
+        self._ck(lib().ns3d_les_train(self._h, iterations, lr, ctypes.byref(v)))
+        return v.value
+
+    def dataset_loss(self) -> float:
+        v = ctypes.c_double()
+        self._ck(lib().ns3d_les_dataset_loss(self._h, ctypes.byref(v)))
+        return v.value
+
+    def weights(self) -> np.ndarray:
+        w = np.empty(self.num_params(), np.float32)
+        self._ck(lib().ns3d_les_weights_host(self._h, _fp(w), 0))
+        return w
+
+    def set_weights(self, w: np.ndarray):
+        w = np.ascontiguousarray(w, dtype=np.float32)
+        self._ck(lib().ns3d_les_weights_host(self._h, _fp(w), 1))
+
+    def gradients(self, u: np.ndarray, tau: np.ndarray):
+        u = np.ascontiguousarray(u, dtype=np.float32)
+        tau = np.ascontiguousarray(tau, dtype=np.float32)
+        g = np.empty(self.num_params(), np.float32)
+        loss = ctypes.c_double()
+        self._ck(lib().ns3d_les_gradients_host(self._h, _fp(u), _fp(tau), ctypes.byref(loss), _fp(g)))
+        return loss.value, g
+
+    def forward(self, u: np.ndarray) -> np.ndarray:
+        u = np.ascontiguousarray(u, dtype=np.float32)
+        out = np.empty((6,) + u.shape[1:], np.float32)
+        self._ck(lib().ns3d_les_forward_host(self._h, _fp(u), _fp(out)))
+        return out

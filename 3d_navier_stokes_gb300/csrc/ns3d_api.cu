@@ -83,13 +83,7 @@ ns3d_status ic_dispatch(Base* impl, int N, const char* name, uint64_t seed, doub
 
 }  // namespace ns3d
 
-struct ns3d_ctx {
-    ns3d_params p;
-    ns3d::Base* impl;
-    cudaStream_t stream;
-    bool own_stream;
-    char err[512];
-};
+#include "ns3d_ctx.h"
 
 static ns3d_status fail(ns3d_ctx* c, ns3d_status s, const char* msg) {
     if (c) snprintf(c->err, sizeof(c->err), "%s", msg);

@@ -10,6 +10,13 @@
 
 namespace ns3d {
 
+// The learned subgrid closure as seen by an engine: tau[6][N^3] from the
+// real-space velocity u[3][N^3], enqueued on stream s (FP32 device arrays).
+struct LesHook {
+    virtual ~LesHook() {}
+    virtual void forward(const float* u, float* tau, int N, cudaStream_t s) = 0;
+};
+
 class Base {
   public:
     Base(const ns3d_params& p, cudaStream_t s) : p_(p), s_(s) { err_[0] = 0; }
@@ -42,6 +49,12 @@ class Base {
     virtual ns3d_status select(int m) = 0;
     virtual void enqueue_step() = 0;
     virtual ns3d_status status() = 0;
+    // learned closure: attach (NULL detaches), step counters, the real-space
+    // velocity for filtering, r2c of a host real-layout velocity
+    virtual ns3d_status attach_les(LesHook* h) = 0;
+    virtual ns3d_status les_counters(long* on, long* off) = 0;
+    virtual const float* real_velocity_f32(ns3d_status* st) = 0;
+    virtual ns3d_status set_state_real_host(const double* u) = 0;
 
     const char* err() const { return err_; }
     void set_err(const char* fmt, ...) {

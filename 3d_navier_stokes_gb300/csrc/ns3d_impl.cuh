@@ -68,7 +68,8 @@ class Impl final : public Base {
     ~Impl() override {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
-                        (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_})
+                        (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
+                        (void*)tau_real_, (void*)sgs_part_})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -175,7 +176,8 @@ class Impl final : public Base {
     template <int INTEG, int MODE>
     void p5x(int m0, int cnt, cx<T>* out) {
         k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
-            Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0));
+            Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0),
+            (les_ && MODE <= X_STAGE4) ? F_ : nullptr);
     }
     template <int MODE>
     void p5(int m0, int cnt, cx<T>* out = nullptr) {
@@ -188,10 +190,32 @@ class Impl final : public Base {
                                                                    use_cfl);
     }
 
+    // -div(tau) of the learned closure for the state at the start of the step
+    // (single run): real-space u, network, r2c of the six tau components,
+    // divergence, energy-budget flag. The term is then held for the 4 stages.
+    void launch_sgs() {
+        p1(U_, 0, 1); p2(0, 1);
+        k_zpass<T, N, 1><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            W_, tw_, real_, nullptr, 0);
+        les_->forward(reinterpret_cast<const float*>(real_), reinterpret_cast<float*>(tau_real_), N, s_);
+        const long long M3 = (long long)N * N * N;
+        for (int h = 0; h < 2; ++h) {
+            k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+                W_, tw_, tau_real_ + h * 3 * M3, nullptr, 0);
+            p4(0, 1);
+            k_xfwd<T, N, INT_IFRK4, X_PLAIN><<<dim3(NTX, G::NKY, 1), TX * PX::P, smem_x(), s_>>>(
+                W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr);
+        }
+        k_sgs_div<T, N><<<kSgsParts, 256, 0, s_>>>(TAU_, U_, F_, sgs_part_);
+        k_sgs_flag<><<<1, 32, 0, s_>>>(sgs_part_, kSgsParts, sd_);
+    }
+    static constexpr int kSgsParts = 512;
+
     // one time step of every member = 4 nonlinear evaluations with fused stage epilogues
     void launch_step() {
         const int cfl = p_.cfl > 0 ? 1 : 0;
         const int M = M_;
+        if (les_) launch_sgs();
         p1(U_, 0, M); p2(0, M); p3(cfl, 0, M);
         if (cfl) tables(1, 0, M);
         p4(0, M); p5<X_STAGE1>(0, M);
@@ -562,6 +586,66 @@ class Impl final : public Base {
     // device pointers for in-library tools
     void* state_ptr() override { return Um(m_); }
 
+    // ----------------------------------------------- learned closure hooks
+    ns3d_status attach_les(LesHook* h) override {
+        if (sizeof(T) != 4 || M_ != 1) {
+            set_err("the learned closure needs a single FP32 run");
+            return NS3D_ERR_INVALID;
+        }
+        if (h) {
+            ns3d_status st = ensure_real();
+            if (st != NS3D_OK) return st;
+            const size_t fb = sizeof(cx<T>) * (size_t)G::FS;
+            if (!TAU_) NS3D_CK(cudaMalloc(&TAU_, 6 * fb));
+            if (!F_) NS3D_CK(cudaMalloc(&F_, 3 * fb));
+            if (!tau_real_) NS3D_CK(cudaMalloc(&tau_real_, sizeof(T) * 6 * (size_t)N * N * N));
+            if (!sgs_part_) NS3D_CK(cudaMalloc(&sgs_part_, sizeof(double) * kSgsParts));
+        }
+        les_ = h;
+        if (graph_exec_) {   // the step graph changes
+            cudaGraphExecDestroy(graph_exec_);
+            graph_exec_ = nullptr;
+        }
+        return NS3D_OK;
+    }
+    ns3d_status les_counters(long* on, long* off) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        if (on) *on = (long)sd_host_->sgs_steps;
+        if (off) *off = (long)sd_host_->sgs_fallbacks;
+        return NS3D_OK;
+    }
+    // real-space velocity of the selected member as [3][N^3] device floats
+    const float* real_velocity_f32(ns3d_status* st) override {
+        if (sizeof(T) != 4) {
+            set_err("real-space velocity export needs an FP32 run");
+            *st = NS3D_ERR_INVALID;
+            return nullptr;
+        }
+        *st = ensure_real();
+        if (*st != NS3D_OK) return nullptr;
+        p1(U_, m_, 1); p2(m_, 1);
+        k_zpass<T, N, 1><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            Wm(m_), tw_, real_, nullptr, 0);
+        *st = cudaGetLastError() == cudaSuccess ? NS3D_OK : NS3D_ERR_CUDA;
+        return reinterpret_cast<const float*>(real_);
+    }
+    // r2c + dealias of a host velocity in the reference real layout
+    ns3d_status set_state_real_host(const double* u) override {
+        ns3d_status st = ensure_real();
+        if (st == NS3D_OK) st = ensure_stage();
+        if (st != NS3D_OK) return st;
+        NS3D_CK(cudaMemcpyAsync(stage_, u, sizeof(double) * 3 * (size_t)N * N * (N + 2), cudaMemcpyHostToDevice, s_));
+        k_real_pack<T, N><<<grid_for((long long)N * N * N), 256, 0, s_>>>(reinterpret_cast<const double*>(stage_),
+                                                                         real_);
+        k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            Wm(m_), tw_, real_, nullptr, 0);
+        p4(m_, 1);
+        p5<X_PLAIN>(m_, 1, U_);
+        NS3D_CK(cudaGetLastError());
+        return reset_forcing_target();
+    }
+
   private:
     cx<T>* U_ = nullptr;
     cx<T>* UT_ = nullptr;
@@ -579,6 +663,11 @@ class Impl final : public Base {
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     int zline_ctas_ = 1;
+    LesHook* les_ = nullptr;       // learned closure (single FP32 run)
+    cx<T>* TAU_ = nullptr;         // tau_ij spectra (6 fields)
+    cx<T>* F_ = nullptr;           // -div(tau) (3 fields)
+    T* tau_real_ = nullptr;        // tau_ij in real space [6][N^3]
+    double* sgs_part_ = nullptr;
     int M_ = 1;                    // members
     int m_ = 0;                    // selected member
     std::vector<ns3d_params> mp_;  // per-member parameters

@@ -105,7 +105,8 @@ struct StepDev {
     unsigned long long umax_bits;    // running max of the stage-1 z pass (bits of T, non-negative)
     long long iters;
     int status;                      // 0 ok; 5 numeric
-    int pad;
+    int sgs_on;                      // learned closure used in this step (energy-budget check passed)
+    long long sgs_steps, sgs_fallbacks;
 };
 
 enum { INT_IFRK4 = 0, INT_RK4CN = 1 };
@@ -584,7 +585,7 @@ template <typename T, int N, int INTEG, int MODE>
 __global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
 k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
        cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
-       const cx<T>* __restrict__ tab) {
+       const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs) {
     using G = Geo<N>;
     using PL = typename Plans<N>::X;
     constexpr int TT = tile_x<T, N>();
@@ -634,6 +635,13 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         if (kx * kx > rem) continue;
         const int k2 = kx * kx + ky * ky + kz * kz;
         cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
+        if (MODE <= X_STAGE4 && sgs && sd->sgs_on) {
+            // learned subgrid term -div(tau), single run only (member 0)
+            const long long q = (long long)i * xs + off;
+            n0 = n0 + sgs[q];
+            n1 = n1 + sgs[G::FS + q];
+            n2 = n2 + sgs[2 * G::FS + q];
+        }
         if (MODE != X_PLAIN) {
             if (k2 > 0) {
                 const T kinv = T(1) / T(k2);
@@ -1081,6 +1089,80 @@ __global__ void k_scale(cx<T>* __restrict__ U, double s) {
     const T sc = T(s);
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x)
         U[q] = U[q] * sc;
+}
+
+}  // namespace ns3d
+
+namespace ns3d {
+
+// ---------------------------------------------------------------------------
+// Learned subgrid closure support (single run, FP32 engines)
+// ---------------------------------------------------------------------------
+// F_i = -i k_j tau_ij (tau components xx, yy, zz, xy, xz, yz) and the
+// per-CTA partials of the energy transfer T = sum_k m Re(u . conj(F)).
+template <typename T, int N>
+__global__ void k_sgs_div(const cx<T>* __restrict__ TAU, const cx<T>* __restrict__ U, cx<T>* __restrict__ F,
+                          double* __restrict__ part) {
+    using G = Geo<N>;
+    __shared__ double red[256];
+    const long long total = (long long)N * N * G::NZP;
+    double s = 0.0;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(q % G::NZP);
+        const long long ij = q / G::NZP;
+        const int kx = kof<N>((int)(ij / N)), ky = kof<N>((int)(ij % N));
+        cx<T> f[3] = {czero<T>(), czero<T>(), czero<T>()};
+        if (kz <= G::KC && kx * kx + ky * ky + kz * kz <= G::KC2) {
+            const cx<T> txx = TAU[q], tyy = TAU[G::FS + q], tzz = TAU[2 * G::FS + q];
+            const cx<T> txy = TAU[3 * G::FS + q], txz = TAU[4 * G::FS + q], tyz = TAU[5 * G::FS + q];
+            const T fx = T(kx), fy = T(ky), fz = T(kz);
+            // -i (k . tau)_i
+            f[0] = mul_mi(txx * fx + txy * fy + txz * fz);
+            f[1] = mul_mi(txy * fx + tyy * fy + tyz * fz);
+            f[2] = mul_mi(txz * fx + tyz * fy + tzz * fz);
+            const double m = kz == 0 ? 1.0 : 2.0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const cx<T> u = U[c * G::FS + q];
+                s += m * ((double)u.x * (double)f[c].x + (double)u.y * (double)f[c].y);
+            }
+        }
+#pragma unroll
+        for (int c = 0; c < 3; ++c) F[c * G::FS + q] = f[c];
+    }
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+// energy-budget check of the closure: keep it for this step only when it
+// removes energy on balance (T <= 0) and is finite; otherwise this step is
+// the plain coarse solve
+template <int Unused = 0>
+__global__ void k_sgs_flag(const double* __restrict__ part, int nparts, StepDev* __restrict__ sd) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double s = 0.0;
+    for (int i = 0; i < nparts; ++i) s += part[i];
+    const int ok = isfinite(s) && s <= 0.0;
+    sd->sgs_on = ok;
+    if (ok) sd->sgs_steps += 1;
+    else sd->sgs_fallbacks += 1;
+}
+
+// reference real layout [N][N][N+2][3] (double) -> device real fields [3][N^3]
+template <typename T, int N>
+__global__ void k_real_pack(const double* __restrict__ u, T* __restrict__ R) {
+    const long long M = (long long)N * N * N;
+    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < M; q += (long long)gridDim.x * blockDim.x) {
+        const long long ij = q / N;
+        const int k = (int)(q % N);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) R[c * M + q] = T(u[(ij * (N + 2) + k) * 3 + c]);
+    }
 }
 
 }  // namespace ns3d

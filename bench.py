@@ -45,6 +45,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble"])
     return ap.parse_args()
 
 
@@ -310,11 +311,53 @@ def s_kernels(pkg, N):
     return k
 
 
+def run_ensemble(args, local):
+    """Config C4: 96 independent FP32 runs (32 x 48^3, 32 x 64^3, 24 x 96^3, 8 x 128^3), each with its own
+    seeded SPECTRUM initial field (k0 ~ U[2, 6]) and nu log-uniform in [5e-4, 5e-3], CFL 0.5, IF-RK4,
+    stepped together (one CUDA graph launch per step). Prints one JSON line."""
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    rng = np.random.default_rng(2024)
+    sizes = [48] * 32 + [64] * 32 + [96] * 24 + [128] * 8
+    k0 = rng.uniform(2.0, 6.0, len(sizes))
+    nu = np.exp(rng.uniform(np.log(5e-4), np.log(5e-3), len(sizes)))
+    members = [dict(N=n, nu=float(v), dt=1e-3, cfl=0.5, precision="fp32", device=local) for n, v in zip(sizes, nu)]
+    ens = pkg.Ensemble(members)
+    for i in range(len(sizes)):
+        ens.InitialConditions(i, "SPECTRUM", seed=i, k0=float(k0[i]))
+    ens.step(args.warmup)
+    torch.cuda.synchronize()
+    clk = Clocks(local)
+    ens.step(args.steps)
+    clocks = clk.stop()
+    ms = ens.last_step_ms()
+    groups, kps = ens.info()
+    pts = sum(n ** 3 for n in sizes)
+    e0 = [ens.measurables(i)[0]["energy"] for i in (0, 32, 64, 88)]
+    line = {"metric": "ensemble grid-pt*RK4-steps/s (96 runs: 32x48^3, 32x64^3, 24x96^3, 8x128^3)",
+            "value": pts * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "batched ensemble, FP32, IF-RK4, CFL 0.5, one graph launch per step",
+                       "members": len(sizes), "launch_groups": groups, "grid_points": pts},
+            "clocks": clocks, "gpu_launches": kps * args.steps,
+            "energy_samples": e0}
+    print(json.dumps(line), flush=True)
+    ens.close()
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
     if args.impl == "reference":
         run_reference(args, ws, rank)
+        return
+    if args.workload == "ensemble":
+        run_ensemble(args, local)
         return
     run_ours(args, ws, rank, local)
 

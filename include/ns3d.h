@@ -169,6 +169,47 @@ ns3d_status ns3d_ensemble_info(ns3d_ensemble* e, int* groups, int* kernels_per_s
 /* device time of the last ns3d_ensemble_step call, milliseconds */
 ns3d_status ns3d_ensemble_last_step_ms(ns3d_ensemble* e, float* ms);
 
+/* r2c + 2/3 dealiasing of a host velocity in the reference real layout
+ * [N][N][N+2][3] into the state (InitialConditions' transform path,
+ * solver.c:1573-1599). */
+ns3d_status ns3d_set_state_real_host(ns3d_ctx* ctx, const double* u);
+
+/* ------------------------------------------------------------------------
+ * Learned subgrid closure (new; no counterpart in the reference). A 3D CNN
+ * (3^3 convolutions 3 -> 32 -> 32 -> 32 -> 6, GELU, circular padding, BF16
+ * weights, FP32 accumulation) maps the box-filtered velocity ubar to the
+ * subgrid stress tau_ij (xx, yy, zz, xy, xz, yz) on an Nc^3 grid (Nc % 8 == 0).
+ * Training pairs come from FP32 runs on a finer grid; attached to a coarse
+ * FP32 run, -div(tau) enters every step unless the energy-budget check finds
+ * that it would add energy, in which case that step is the plain solve.
+ * ------------------------------------------------------------------------ */
+typedef struct ns3d_les ns3d_les;
+int ns3d_les_num_params(void);
+ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out);
+ns3d_status ns3d_les_destroy(ns3d_les* l);
+const char* ns3d_les_last_error(const ns3d_les* l);
+/* box-filter the current state of a fine FP32 context (N = F * Nc) into the dataset */
+ns3d_status ns3d_les_add_snapshot(ns3d_les* l, ns3d_ctx* fine);
+ns3d_status ns3d_les_dataset_size(ns3d_les* l, int* count);
+/* box-filtered velocity of a fine context, reference real layout [Nc][Nc][Nc+2][3] */
+ns3d_status ns3d_les_filtered_velocity_host(ns3d_les* l, ns3d_ctx* fine, double* ubar);
+/* input scale s_in and output scale s_out (default: RMS of ubar over the dataset, its square) */
+ns3d_status ns3d_les_set_scales(ns3d_les* l, double s_in, double s_out);
+ns3d_status ns3d_les_get_scales(ns3d_les* l, double* s_in, double* s_out);
+/* Adam over random dataset samples; mean_loss = mean MSE of the last 10% of iterations */
+ns3d_status ns3d_les_train(ns3d_les* l, int iterations, double lr, double* mean_loss);
+ns3d_status ns3d_les_dataset_loss(ns3d_les* l, double* mean_loss);
+/* FP32 master weights (ns3d_les_num_params floats), get (set = 0) or set */
+ns3d_status ns3d_les_weights_host(ns3d_les* l, float* w, int set);
+/* loss and weight gradients for one sample (u [3][Nc^3], tau [6][Nc^3] host floats) */
+ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* tau, double* loss, float* grads);
+/* tau = network(u) in physical units */
+ns3d_status ns3d_les_forward_host(ns3d_les* l, const float* u, float* tau);
+/* attach the closure to a coarse FP32 context of grid Nc (NULL detaches) */
+ns3d_status ns3d_les_attach(ns3d_ctx* coarse, ns3d_les* l);
+/* steps taken with the closure and steps that fell back to the plain solve */
+ns3d_status ns3d_les_counters(ns3d_ctx* coarse, long* closure_steps, long* fallback_steps);
+
 /* Instrumentation for benchmarks: the stream the context runs on, the number
  * of kernels one step launches, and the device time of the last ns3d_step
  * call (CUDA events on the context stream), in milliseconds. */
