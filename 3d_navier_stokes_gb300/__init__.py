@@ -26,8 +26,9 @@ _lib = None
 
 OK, ERR_INVALID, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_NUMERIC, ERR_TIMEOUT = range(7)
 FP64, FP32 = 0, 1
-IFRK4, RK4CN = 0, 1
+IFRK4, RK4CN, RK5CN, DP5CN = 0, 1, 2, 3
 FORCE_NONE, FORCE_SHELL = 0, 1
+_INTEG = {"ifrk4": IFRK4, "rk4cn": RK4CN, "rk5cn": RK5CN, "dp5cn": DP5CN}
 
 # every symbol include/ns3d.h declares
 EXPORTS = (
@@ -44,7 +45,7 @@ EXPORTS = (
     "ns3d_les_num_params", "ns3d_les_create", "ns3d_les_destroy", "ns3d_les_last_error", "ns3d_les_add_snapshot",
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
-    "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters",
+    "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
 )
 
 
@@ -135,6 +136,10 @@ def lib():
         L.ns3d_set_forcing_target.argtypes = [P, ctypes.c_double]
         L.ns3d_max_speed_sum.restype = I
         L.ns3d_max_speed_sum.argtypes = [P, D]
+        L.ns3d_set_dp_tolerances.restype = I
+        L.ns3d_set_dp_tolerances.argtypes = [P, ctypes.c_double, ctypes.c_double]
+        L.ns3d_dp_stats.restype = I
+        L.ns3d_dp_stats.argtypes = [P, D, ctypes.POINTER(ctypes.c_long)]
         L.ns3d_stream.restype = P
         L.ns3d_stream.argtypes = [P]
         L.ns3d_kernels_per_step.restype = I
@@ -241,7 +246,7 @@ class Solver:
                  forcing: str | None = None, force_k: int = 2, device: int = 0, stream: int | None = None):
         self.N = N
         self.precision = precision
-        integ = {"ifrk4": IFRK4, "rk4cn": RK4CN}[integrator.lower()]
+        integ = _INTEG[integrator.lower()]
         prec = {"fp64": FP64, "fp32": FP32}[precision.lower()]
         force = FORCE_SHELL if (forcing or "").upper() in ("SHELL", "ENERGY_SHELL") else FORCE_NONE
         p = Params(N, nu, dt, t0, visc_pow, integ, prec, cfl, force, force_k, device, stream)
@@ -360,6 +365,16 @@ class Solver:
         self._ck(lib().ns3d_max_speed_sum(self._h, ctypes.byref(v)))
         return v.value
 
+    def set_dp_tolerances(self, atol: float, rtol: float):
+        """DP5CN error tolerances (DP_ABS_TOL, DP_REL_TOL; default 1e-7 each)."""
+        self._ck(lib().ns3d_set_dp_tolerances(self._h, atol, rtol))
+
+    def dp_stats(self):
+        """(error norm of the last DP5CN attempt, rejected attempts so far)"""
+        e, r = ctypes.c_double(), ctypes.c_long()
+        self._ck(lib().ns3d_dp_stats(self._h, ctypes.byref(e), ctypes.byref(r)))
+        return e.value, r.value
+
     # ---------------------------------------------------- instrumentation
     @property
     def stream(self) -> int:
@@ -385,7 +400,7 @@ class Solver:
 
 def _params(N, nu=1.0, dt=1e-3, t0=0.0, visc_pow=1, integrator="ifrk4", precision="fp64", cfl=0.0,
             forcing=None, force_k=2, device=0, stream=None):
-    integ = {"ifrk4": IFRK4, "rk4cn": RK4CN}[integrator.lower()]
+    integ = _INTEG[integrator.lower()]
     prec = {"fp64": FP64, "fp32": FP32}[precision.lower()]
     force = FORCE_SHELL if (forcing or "").upper() in ("SHELL", "ENERGY_SHELL") else FORCE_NONE
     return Params(N, nu, dt, t0, visc_pow, integ, prec, cfl, force, force_k, device, stream)

@@ -124,7 +124,8 @@ ns3d_status ns3d_create(const ns3d_params* p, ns3d_ctx** out) {
     if (!ns3d::supported_n(p->N)) return NS3D_ERR_UNSUPPORTED;
     if (!(p->nu > 0) || !(p->dt > 0) || p->t0 < 0) return NS3D_ERR_INVALID;
     if (p->visc_pow != 1 && p->visc_pow != 2) return NS3D_ERR_INVALID;
-    if (p->integrator != NS3D_IFRK4 && p->integrator != NS3D_RK4CN) return NS3D_ERR_INVALID;
+    if (p->integrator < NS3D_IFRK4 || p->integrator > NS3D_DP5CN) return NS3D_ERR_INVALID;
+    if (p->integrator == NS3D_DP5CN && p->cfl > 0) return NS3D_ERR_INVALID;   // DP5CN chooses its own step
     if (p->precision != NS3D_FP64 && p->precision != NS3D_FP32) return NS3D_ERR_INVALID;
     if (p->forcing != NS3D_FORCE_NONE && p->forcing != NS3D_FORCE_SHELL) return NS3D_ERR_INVALID;
     if (p->forcing == NS3D_FORCE_SHELL && (p->force_k < 1 || p->force_k > p->N / 3)) return NS3D_ERR_INVALID;
@@ -253,6 +254,16 @@ ns3d_status ns3d_get_forcing_target(ns3d_ctx* c, double* e) {
 ns3d_status ns3d_set_forcing_target(ns3d_ctx* c, double e) {
     if (!c || e < 0) return NS3D_ERR_INVALID;
     return pass(c, c->impl->set_forcing_target(e));
+}
+
+ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* c, double atol, double rtol) {
+    if (!c || !(atol > 0) || !(rtol >= 0)) return NS3D_ERR_INVALID;
+    return pass(c, c->impl->set_dp_tolerances(atol, rtol));
+}
+
+ns3d_status ns3d_dp_stats(ns3d_ctx* c, double* last_err, long* rejects) {
+    if (!c) return NS3D_ERR_INVALID;
+    return pass(c, c->impl->dp_stats(last_err, rejects));
 }
 
 ns3d_status ns3d_max_speed_sum(ns3d_ctx* c, double* umax) {

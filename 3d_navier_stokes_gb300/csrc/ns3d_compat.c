@@ -34,9 +34,10 @@ static ns3d_params params_from_sys(double dt) {
     p.dt = dt > 0 ? dt : sys_vars->dt;
     p.t0 = sys_vars->t0;
     p.visc_pow = sys_vars->hyper_visc ? 2 : 1;
-    p.integrator = sys_vars->integrator == 1 ? NS3D_RK4CN : NS3D_IFRK4;
+    p.integrator = (sys_vars->integrator >= NS3D_RK4CN && sys_vars->integrator <= NS3D_DP5CN) ? sys_vars->integrator
+                                                                                             : NS3D_IFRK4;
     p.precision = sys_vars->precision == 1 ? NS3D_FP32 : NS3D_FP64;
-    p.cfl = sys_vars->adaptive_step ? sys_vars->CFL_CONST : 0.0;
+    p.cfl = (sys_vars->adaptive_step && p.integrator != NS3D_DP5CN) ? sys_vars->CFL_CONST : 0.0;
     p.forcing = strcmp(sys_vars->forcing, "SHELL") == 0 ? NS3D_FORCE_SHELL : NS3D_FORCE_NONE;
     p.force_k = sys_vars->force_k > 0 ? sys_vars->force_k : 2;
     p.device = 0;
@@ -115,6 +116,34 @@ void RK4Step(const double dt, const long int* N, const ptrdiff_t local_Nx, RK_da
     if (s == NS3D_OK && cur_dt != dt && !sys_vars->adaptive_step) s = ns3d_set_time(c, t, dt, it);
     if (s == NS3D_OK) s = ns3d_step_host(c, (const double*)run_data->u_hat, (double*)run_data->u_hat);
     if (s != NS3D_OK) die("RK4Step", s);
+}
+
+/* RK5DPStep (solver.c:217-421): one RK5CN step (integrator 2), or one accepted
+   Dormand-Prince step (integrator 3): the step-size control of SpectralSolve
+   (solver.c:134-154) runs inside, and sys_vars->dt and sys_vars->t receive the
+   next step size and the new time. */
+void RK5DPStep(const double dt, const long int* N, const int iters, const ptrdiff_t local_Nx, RK_data_struct* RK_data) {
+    (void)N;
+    (void)iters;
+    (void)local_Nx;
+    (void)RK_data;
+    if (!sys_vars || (sys_vars->integrator != NS3D_RK5CN && sys_vars->integrator != NS3D_DP5CN)) {
+        fprintf(stderr, "\n[ERROR] --- RK5DPStep needs sys_vars->integrator 2 (RK5) or 3 (DPRK5)\n-->> Exiting!!!\n");
+        exit(1);
+    }
+    ns3d_ctx* c = ctx_for(dt);
+    double t = 0, cur_dt = 0;
+    long it = 0;
+    ns3d_status s = ns3d_get_time(c, &t, &cur_dt, &it);
+    if (s == NS3D_OK && sys_vars->integrator == NS3D_RK5CN && cur_dt != dt && !sys_vars->adaptive_step)
+        s = ns3d_set_time(c, t, dt, it);
+    if (s == NS3D_OK) s = ns3d_step_host(c, (const double*)run_data->u_hat, (double*)run_data->u_hat);
+    if (s == NS3D_OK && sys_vars->integrator == NS3D_DP5CN) {
+        s = ns3d_get_time(c, &t, &cur_dt, &it);
+        sys_vars->dt = cur_dt;
+        sys_vars->t = t;
+    }
+    if (s != NS3D_OK) die("RK5DPStep", s);
 }
 
 void NonlinearRHSBatch(ns3d_fftw_complex* u_hat, ns3d_fftw_complex* dw_hat_dt, double* curl, double* u,

@@ -99,7 +99,7 @@ ns3d_status ns3d_ensemble_create(const ns3d_params* members, int count, ns3d_ens
         const ns3d_params* p = &members[i];
         if (p->N <= 2 || (p->N % 2) || !(p->nu > 0) || !(p->dt > 0) || p->t0 < 0) return NS3D_ERR_INVALID;
         if (!ns3d::supported_n(p->N)) return NS3D_ERR_UNSUPPORTED;
-        if ((p->visc_pow != 1 && p->visc_pow != 2) || (p->integrator != NS3D_IFRK4 && p->integrator != NS3D_RK4CN) ||
+        if ((p->visc_pow != 1 && p->visc_pow != 2) || (p->integrator < NS3D_IFRK4 || p->integrator > NS3D_RK5CN) ||
             (p->precision != NS3D_FP64 && p->precision != NS3D_FP32) || p->cfl < 0 ||
             (p->forcing != NS3D_FORCE_NONE && p->forcing != NS3D_FORCE_SHELL) ||
             (p->forcing == NS3D_FORCE_SHELL && (p->force_k < 1 || p->force_k > p->N / 3)) ||

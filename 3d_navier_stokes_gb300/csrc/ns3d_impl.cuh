@@ -69,7 +69,7 @@ class Impl final : public Base {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
                         (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
-                        (void*)tau_real_, (void*)sgs_part_})
+                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -77,7 +77,13 @@ class Impl final : public Base {
         if (ev1_) cudaEventDestroy(ev1_);
     }
 
-    int kernels_per_step() const override { return 4 * 5 + (p_.cfl > 0 ? 1 : 0) + 1; }
+    bool rk5() const { return p_.integrator == INT_RK5CN || p_.integrator == INT_DP5CN; }
+    bool dp5() const { return p_.integrator == INT_DP5CN; }
+    int kernels_per_step() const override {
+        if (dp5()) return 1 + 7 * 5 + 3;
+        if (rk5()) return 6 * 5 + (p_.cfl > 0 ? 1 : 0) + 1;
+        return 4 * 5 + (p_.cfl > 0 ? 1 : 0) + 1;
+    }
 
     ns3d_status init() override {
         const size_t fb = sizeof(cx<T>) * (size_t)G::FS * M_;
@@ -88,6 +94,12 @@ class Impl final : public Base {
         NS3D_CK(cudaMemsetAsync(U_, 0, 3 * fb, s_));
         NS3D_CK(cudaMemsetAsync(UT_, 0, 3 * fb, s_));
         NS3D_CK(cudaMemsetAsync(ACC_, 0, 3 * fb, s_));
+        if (rk5()) {
+            // stored stages k_1..k_6 of the RK5 family, and the DP5CN error partial sums
+            NS3D_CK(cudaMalloc(&K_, 18 * fb));
+            NS3D_CK(cudaMemsetAsync(K_, 0, 18 * fb, s_));
+            NS3D_CK(cudaMalloc(&dpart_, sizeof(double) * 3 * (size_t)NTX * G::NKY * M_));
+        }
         NS3D_CK(cudaMalloc(&tw_, sizeof(cx<T>) * N));
         NS3D_CK(cudaMalloc(&tab_, sizeof(cx<T>) * (G::KC2 + 1) * M_));
         NS3D_CK(cudaMalloc(&part_, sizeof(double) * NMEAS * MWIDTH));
@@ -107,6 +119,7 @@ class Impl final : public Base {
         for (int m = 0; m < M_; ++m) {
             StepDev sd{};
             sd.t = mp_[m].t0; sd.dt = mp_[m].dt; sd.t0 = mp_[m].t0; sd.nu = mp_[m].nu; sd.cfl = mp_[m].cfl;
+            sd.dp_atol = 1e-7; sd.dp_rtol = 1e-7;   // DP_ABS_TOL, DP_REL_TOL (data_types.h:123-124)
             sd_host_[m] = sd;
         }
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
@@ -127,6 +140,8 @@ class Impl final : public Base {
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
+        NS3D_CK(cudaFuncSetAttribute(k_xfwd<T, N, INT_TAB, X_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     smem_x()));
         tables(0, 0, M_);
         NS3D_CK(cudaGetLastError());
         NS3D_CK(cudaStreamSynchronize(s_));
@@ -177,7 +192,13 @@ class Impl final : public Base {
     void p5x(int m0, int cnt, cx<T>* out) {
         k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
             Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0),
-            (les_ && MODE <= X_STAGE4) ? F_ : nullptr);
+            (les_ && MODE <= X_STAGE4) ? F_ : nullptr, nullptr, nullptr, RkStage{});
+    }
+    // RK5-family stage epilogue s (0-based) of members [m0, m0 + cnt)
+    void p5tab(int s, int m0, int cnt) {
+        k_xfwd<T, N, INT_TAB, X_STAGE1><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+            Wm(m0), Um(m0), UTm(m0), ACCm(m0), tw_, sdm(m0), tabm(m0), les_ ? F_ : nullptr,
+            K_ + (size_t)m0 * 18 * G::FS, dpart_ + (size_t)m0 * 3 * NTX * G::NKY, rk_stage(s, dp5()));
     }
     template <int MODE>
     void p5(int m0, int cnt, cx<T>* out = nullptr) {
@@ -204,15 +225,76 @@ class Impl final : public Base {
                 W_, tw_, tau_real_ + h * 3 * M3, nullptr, 0);
             p4(0, 1);
             k_xfwd<T, N, INT_IFRK4, X_PLAIN><<<dim3(NTX, G::NKY, 1), TX * PX::P, smem_x(), s_>>>(
-                W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr);
+                W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr, nullptr, nullptr, RkStage{});
         }
         k_sgs_div<T, N><<<kSgsParts, 256, 0, s_>>>(TAU_, U_, F_, sgs_part_);
         k_sgs_flag<><<<1, 32, 0, s_>>>(sgs_part_, kSgsParts, sd_);
     }
     static constexpr int kSgsParts = 512;
 
+    // Dormand & Prince (1980) RK5(4)7M coefficients. The reference's table
+    // (solver.c:34-42) holds the same numbers except a32, 1/2 there: the
+    // published 9/40 is the value that satisfies a31 + a32 = c3 = 3/10.
+    static RkStage rk_stage(int s, bool dp) {
+        static const double A[7][6] = {
+            {0, 0, 0, 0, 0, 0},
+            {1.0 / 5.0, 0, 0, 0, 0, 0},
+            {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+            {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+            {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+            {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+            {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+        static const double B[7] = {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0, 0};
+        static const double BS[7] = {5179.0 / 57600.0, 0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0,
+                                     187.0 / 2100.0, 1.0 / 40.0};
+        RkStage r{};
+        const int last = dp ? 6 : 5;
+        r.nk = s;
+        r.store = s < last ? s : -1;
+        if (s < last) {
+            r.kind = 0;
+            for (int j = 0; j < s; ++j) r.c[j] = A[s + 1][j];
+            r.c_cur = A[s + 1][s];
+        } else {
+            r.kind = dp ? 2 : 1;
+            for (int j = 0; j < s; ++j) {
+                r.c[j] = B[j];
+                if (dp) r.e[j] = B[j] - BS[j];
+            }
+            r.c_cur = B[s];
+            if (dp) r.e_cur = B[s] - BS[s];
+        }
+        return r;
+    }
+
+    // one RK5CN step or DP5CN attempt of every member: 6 or 7 nonlinear
+    // evaluations, each ending in its tableau epilogue
+    void launch_step_rk5() {
+        const bool dp = dp5();
+        const int cfl = (!dp && p_.cfl > 0) ? 1 : 0;
+        const int M = M_;
+        const int S = dp ? 7 : 6;
+        if (les_) launch_sgs();
+        if (dp) tables(0, 0, M);
+        for (int s = 0; s < S; ++s) {
+            p1(s == 0 ? U_ : UT_, 0, M); p2(0, M); p3(s == 0 ? cfl : 0, 0, M);
+            if (s == 0 && cfl) tables(1, 0, M);
+            p4(0, M);
+            p5tab(s, 0, M);
+        }
+        if (dp) {
+            k_dp_ctl<T, N><<<M, 256, 0, s_>>>(dpart_, NTX * G::NKY, sd_);
+            k_dp_commit<T, N><<<dim3(grid_for((long long)N * N * G::NZP), M), 256, 0, s_>>>(U_, ACC_, sd_);
+        }
+        k_step_end<T, N><<<M, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl, dp ? 1 : 0);
+    }
+
     // one time step of every member = 4 nonlinear evaluations with fused stage epilogues
     void launch_step() {
+        if (rk5()) {
+            launch_step_rk5();
+            return;
+        }
         const int cfl = p_.cfl > 0 ? 1 : 0;
         const int M = M_;
         if (les_) launch_sgs();
@@ -222,7 +304,7 @@ class Impl final : public Base {
         p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE2>(0, M);
         p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE3>(0, M);
         p1(UT_, 0, M); p2(0, M); p3(0, 0, M); p4(0, M); p5<X_STAGE4>(0, M);
-        k_step_end<T, N><<<M, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+        k_step_end<T, N><<<M, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl, 0);
     }
 
     ns3d_status build_graph() {
@@ -249,10 +331,29 @@ class Impl final : public Base {
         if (nsteps <= 0) return NS3D_OK;
         ns3d_status st = build_graph();
         if (st != NS3D_OK) return st;
+        if (dp5()) return step_dp5(nsteps);
         NS3D_CK(cudaEventRecord(ev0_, s_));
         for (int k = 0; k < nsteps; ++k) NS3D_CK(cudaGraphLaunch(graph_exec_, s_));
         NS3D_CK(cudaEventRecord(ev1_, s_));
         return check_status();
+    }
+    // DP5CN (single run): one graph launch per attempt; launches continue
+    // until nsteps attempts were accepted. k_dp_ctl ends the run with
+    // kStatusDpFail after kDpMaxTry rejections in a row, so the loop ends.
+    ns3d_status step_dp5(int nsteps) {
+        ns3d_status st = check_status();
+        if (st != NS3D_OK) return st;
+        const long long start = sd_host_[0].iters;
+        long long done = 0;
+        NS3D_CK(cudaEventRecord(ev0_, s_));
+        while (done < nsteps) {
+            for (long long k = done; k < nsteps; ++k) NS3D_CK(cudaGraphLaunch(graph_exec_, s_));
+            NS3D_CK(cudaEventRecord(ev1_, s_));
+            st = check_status();
+            if (st != NS3D_OK) return st;
+            done = sd_host_[0].iters - start;
+        }
+        return NS3D_OK;
     }
 
     ns3d_status check_status() {
@@ -263,6 +364,11 @@ class Impl final : public Base {
             if (sd_host_[m].status == kStatusTimeout) {
                 set_err("member %d: a bounded wait for an asynchronous copy gave up at step %lld", m, sd_host_[m].iters);
                 return NS3D_ERR_TIMEOUT;
+            }
+            if (sd_host_[m].status == kStatusDpFail) {
+                set_err("member %d: DP5CN step rejected %d times in a row at step %lld (error norm %g, dt %g)", m,
+                        kDpMaxTry, sd_host_[m].iters, sd_host_[m].dp_err, sd_host_[m].dt);
+                return NS3D_ERR_NUMERIC;
             }
             if (sd_host_[m].status != 0) {
                 set_err("member %d: numeric health check failed at step %lld (NaN/Inf energy or speed)", m,
@@ -280,6 +386,10 @@ class Impl final : public Base {
 
     // per-kernel-class timing of `reps` steps launched one kernel at a time
     ns3d_status profile(int reps, const char** names, float* ms, double* bytes, int maxc, int* count) override {
+        if (rk5()) {
+            set_err("per-kernel profile covers the RK4-family step");
+            return NS3D_ERR_UNSUPPORTED;
+        }
         static const char* kNames[6] = {"k_xinv", "k_ypass_inv", zline_ok<T, N>() ? "k_zline" : "k_zpass", "k_ypass_fwd", "k_xfwd", "k_misc"};
         std::vector<cudaEvent_t> ev(2 * 6 * 4 + 2);
         for (auto& e : ev) NS3D_CK(cudaEventCreate(&e));
@@ -300,7 +410,7 @@ class Impl final : public Base {
                 else if (s == 2) p5<X_STAGE3>(0, M); else p5<X_STAGE4>(0, M);
                 NS3D_CK(cudaEventRecord(ev[q++], s_));
             }
-            k_step_end<T, N><<<M_, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl);
+            k_step_end<T, N><<<M_, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl, 0);
             NS3D_CK(cudaEventRecord(ev[q++], s_));
             NS3D_CK(cudaStreamSynchronize(s_));
             q = 0;
@@ -568,6 +678,24 @@ class Impl final : public Base {
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
+    ns3d_status set_dp_tolerances(double atol, double rtol) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev) * M_, cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        for (int m = 0; m < M_; ++m) {
+            sd_host_[m].dp_atol = atol;
+            sd_host_[m].dp_rtol = rtol;
+        }
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+    ns3d_status dp_stats(double* err, long* rejects) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        if (err) *err = sd_host_->dp_err;
+        if (rejects) *rejects = (long)sd_host_->dp_rejects;
+        return NS3D_OK;
+    }
     ns3d_status get_forcing_target(double* e) override {
         NS3D_CK(cudaMemcpyAsync(sd_host_, sdm(m_), sizeof(StepDev), cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
@@ -668,6 +796,8 @@ class Impl final : public Base {
     cx<T>* F_ = nullptr;           // -div(tau) (3 fields)
     T* tau_real_ = nullptr;        // tau_ij in real space [6][N^3]
     double* sgs_part_ = nullptr;
+    cx<T>* K_ = nullptr;           // RK5 family: stored stages [member][6][3]
+    double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]
     int M_ = 1;                    // members
     int m_ = 0;                    // selected member
     std::vector<ns3d_params> mp_;  // per-member parameters

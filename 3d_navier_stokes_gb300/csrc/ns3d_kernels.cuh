@@ -107,9 +107,34 @@ struct StepDev {
     int status;                      // 0 ok; 5 numeric
     int sgs_on;                      // learned closure used in this step (energy-budget check passed)
     long long sgs_steps, sgs_fallbacks;
+    // Dormand-Prince step control (DP5CN)
+    double dp_atol, dp_rtol;         // error tolerances
+    double dp_err;                   // error norm of the last attempt
+    double dp_h;                     // step size of the last attempt
+    int dp_accept;                   // last attempt accepted
+    int dp_tries;                    // consecutive rejected attempts
+    long long dp_rejects;            // rejected attempts so far
 };
 
-enum { INT_IFRK4 = 0, INT_RK4CN = 1 };
+enum { INT_IFRK4 = 0, INT_RK4CN = 1, INT_RK5CN = 2, INT_DP5CN = 3 };
+// k_xfwd template tag of the tableau-driven epilogue (RK5CN, DP5CN)
+enum { INT_TAB = 4 };
+constexpr int kStatusDpFail = 7;     // a DP5CN step was rejected kDpMaxTry times in a row
+constexpr int kDpMaxTry = 50;        // DP_MAX_TRY (data_types.h:128)
+
+// One stage epilogue of the RK5 family (RK5DPStep, solver.c:217-421): with k
+// the projected RHS just computed and K_j the stored earlier stages,
+//   kind 0: UT = U + h (sum_{j<nk} c_j K_j + c_cur k)              next stage input
+//   kind 1: U  = a U + b (sum c_j K_j + c_cur k)                    RK5CN update
+//   kind 2: ACC = a U + b (sum c_j K_j + c_cur k)                   DP5CN trial
+//           err_d += |b (sum e_j K_j + e_cur k)|^2 / den_d^2,  den_d = atol + max(|U|, |ACC|) rtol
+// with (a, b) = ((2-D)/(2+D), 2h/(2+D)) from the step table; k is stored
+// into K_store when store >= 0.
+struct RkStage {
+    int kind, store, nk, pad;
+    double c[6], c_cur;
+    double e[6], e_cur;
+};
 // P5 modes
 enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAIN = 9 };
 
@@ -579,13 +604,16 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
 // P5: forward FFT along x of the 3 product fields, then per mode the Leray
 // projection, dealias mask and RK stage update. grid (ntile, NKY).
 // tab[k2] holds (E_half, E_full) for IF-RK4 or (a, b) = ((2-D)/(2+D),
-// 2h/(2+D)) for RK4CN stage 4, computed in FP64 and rounded to T.
+// 2h/(2+D)) for the Crank-Nicolson updates, computed in FP64 and rounded to
+// T. INTEG = INT_TAB runs the RkStage epilogue of the RK5 family; its DP5CN
+// error partial sums go to dpart[member][block][3] in a fixed order.
 // ---------------------------------------------------------------------------
 template <typename T, int N, int INTEG, int MODE>
 __global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
 k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
        cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
-       const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs) {
+       const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs, cx<T>* __restrict__ K,
+       double* __restrict__ dpart, const RkStage rs) {
     using G = Geo<N>;
     using PL = typename Plans<N>::X;
     constexpr int TT = tile_x<T, N>();
@@ -605,9 +633,16 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         ACC += mem * 3 * G::FS;
         sd += mem;
         tab += mem * (G::KC2 + 1);
+        if (INTEG == INT_TAB) {
+            K += mem * 18 * G::FS;
+            dpart += (mem * gridDim.y * gridDim.x + (long long)blockIdx.y * gridDim.x + blockIdx.x) * 3;
+        }
     }
     const int kz0 = blockIdx.x * TT;
-    if (ky * ky + kz0 * kz0 > G::KC2) return;
+    if (ky * ky + kz0 * kz0 > G::KC2) {
+        if (INTEG == INT_TAB && rs.kind == 2 && threadIdx.x < 3) dpart[threadIdx.x] = 0.0;
+        return;
+    }
     const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
     const long long off = (long long)j * G::NZP + kz;
     const long long xs = (long long)N * G::NZP;
@@ -623,16 +658,17 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) PL::fwd(F[c], sbuf, p, tw, sidx, sync);
-    if (!colok) return;
+    if (INTEG != INT_TAB && !colok) return;
 
     T h = T(0);
     if (MODE <= X_STAGE4) h = T(sd->dt);
     const int rem = G::KC2 - ky * ky - kz * kz;
+    double es[3] = {0.0, 0.0, 0.0};   // DP5CN error partial sums
 #pragma unroll
     for (int s = 0; s < E; ++s) {
         const int i = p + P * s;
         const int kx = kof<N>(i);
-        if (kx * kx > rem) continue;
+        if (!colok || kx * kx > rem) continue;
         const int k2 = kx * kx + ky * ky + kz * kz;
         cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
         if (MODE <= X_STAGE4 && sgs && sd->sgs_on) {
@@ -658,6 +694,39 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         if (MODE == X_RHS || MODE == X_PLAIN) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) ACC[c * G::FS + idx] = nn[c];
+            continue;
+        }
+        if constexpr (INTEG == INT_TAB) {
+            const cx<T> ab = ldg(&tab[k2]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                const long long q = c * G::FS + idx;
+                cx<T> acc = nn[c] * T(rs.c_cur);
+                cx<T> ea = nn[c] * T(rs.e_cur);
+#pragma unroll
+                for (int jj = 0; jj < 6; ++jj) {
+                    if (jj < rs.nk && (rs.c[jj] != 0.0 || rs.e[jj] != 0.0)) {
+                        const cx<T> kj = K[(long long)jj * 3 * G::FS + q];
+                        acc = acc + kj * T(rs.c[jj]);
+                        ea = ea + kj * T(rs.e[jj]);
+                    }
+                }
+                if (rs.store >= 0) K[(long long)rs.store * 3 * G::FS + q] = nn[c];
+                const cx<T> u = U[q];
+                if (rs.kind == 0) {
+                    UT[q] = u + acc * h;
+                } else if (rs.kind == 1) {
+                    U[q] = u * ab.x + acc * ab.y;
+                } else {
+                    const cx<T> un = u * ab.x + acc * ab.y;
+                    ACC[q] = un;
+                    const cx<T> df = ea * ab.y;
+                    const double m0 = sqrt((double)u.x * u.x + (double)u.y * u.y);
+                    const double m1 = sqrt((double)un.x * un.x + (double)un.y * un.y);
+                    const double den = sd->dp_atol + (m0 > m1 ? m0 : m1) * sd->dp_rtol;
+                    es[c] += ((double)df.x * df.x + (double)df.y * df.y) / (den * den);
+                }
+            }
             continue;
         }
         if (INTEG == INT_IFRK4) {
@@ -699,6 +768,34 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
                     const cx<T> ab = ldg(&tab[k2]);
                     U[q] = U[q] * ab.x + (ACC[q] + nn[c] * (T(1) / T(6))) * ab.y;
                 }
+            }
+        }
+    }
+    if constexpr (INTEG == INT_TAB) {
+        if (rs.kind == 2) {
+            // fixed-order block reduction: warp shuffles (full warps; the
+            // block size is a power of two), then the warps' sums in order;
+            // blocks of fewer than 32 threads add their threads in order
+            __shared__ double red[32][3];
+            const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+            const bool full = blockDim.x >= 32;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                double v = es[c];
+                if (full) {
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+                    if (lane == 0) red[wid][c] = v;
+                } else {
+                    red[threadIdx.x][c] = v;
+                }
+            }
+            __syncthreads();
+            if (threadIdx.x < 3) {
+                const int n = full ? (int)(blockDim.x >> 5) : (int)blockDim.x;
+                double v = 0.0;
+                for (int w = 0; w < n; ++w) v += red[w][threadIdx.x];
+                dpart[threadIdx.x] = v;
             }
         }
     }
@@ -748,12 +845,14 @@ __global__ void k_tables(cx<T>* __restrict__ tab, StepDev* __restrict__ sd, int 
 // (solver.c:193). One CTA of 256 threads; deterministic FP64 reduction.
 // ---------------------------------------------------------------------------
 template <typename T, int N>
-__global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int force_k, int use_cfl) {
+__global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int force_k, int use_cfl, int dp) {
     using G = Geo<N>;
     U += (long long)blockIdx.x * 3 * G::FS;   // one CTA per ensemble member
     sd += blockIdx.x;
     __shared__ double red[256];
-    const int kb = force_k;
+    // a rejected DP5CN attempt leaves the state, the time and the forcing alone
+    const bool rejected = dp && !sd->dp_accept;
+    const int kb = rejected ? 0 : force_k;
     const int side = 2 * kb + 1;
     const int nbox = side * side * (kb + 1);
     const long long k2max = (long long)kb * (kb + 1);
@@ -794,11 +893,89 @@ __global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int 
         }
     }
     if (threadIdx.x == 0) {
-        sd->iters += 1;
-        if (use_cfl) sd->t += sd->dt;
-        else sd->t = sd->t0 + (double)sd->iters * sd->dt;
+        if (dp) {
+            if (!rejected) {
+                sd->iters += 1;
+                sd->t += sd->dp_h;
+            }
+        } else {
+            sd->iters += 1;
+            if (use_cfl) sd->t += sd->dt;
+            else sd->t = sd->t0 + (double)sd->iters * sd->dt;
+        }
         if (!isfinite(en)) sd->status = 5;
         sd->umax_bits = 0ull;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// DP5CN step control (SpectralSolve, solver.c:134-154, with D15/D18 fixed):
+// err = max_d sqrt(sum_d / (N N (N/2+1))) from the per-block partial sums in
+// a fixed order; accept when err <= 1; either way the next attempt uses
+// h min(1.5, max(0.01, 0.8 err^(-1/5))). One CTA of 256 threads per member.
+// ---------------------------------------------------------------------------
+template <typename T, int N>
+__global__ void k_dp_ctl(const double* __restrict__ dpart, int nparts, StepDev* __restrict__ sd) {
+    __shared__ double red[3][256];
+    sd += blockIdx.x;
+    dpart += (long long)blockIdx.x * nparts * 3;
+    double v[3] = {0.0, 0.0, 0.0};
+    for (int q = threadIdx.x; q < nparts; q += blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[c] += dpart[3 * q + c];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) red[c][threadIdx.x] = v[c];
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) red[c][threadIdx.x] += red[c][threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double nm = (double)N * N * (N / 2 + 1);
+        double err = sqrt(red[0][0] / nm);
+        err = fmax(err, sqrt(red[1][0] / nm));
+        err = fmax(err, sqrt(red[2][0] / nm));
+        if (!(red[0][0] == red[0][0]) || !(red[1][0] == red[1][0]) || !(red[2][0] == red[2][0])) err = NAN;
+        double fac = 0.8 * pow(1.0 / err, 0.2);
+        fac = fac < 0.01 ? 0.01 : fac;
+        fac = fac > 1.5 ? 1.5 : fac;
+        const double h = sd->dt;
+        sd->dp_err = err;
+        sd->dp_h = h;
+        sd->dt = h * fac;
+        if (err <= 1.0) {
+            sd->dp_accept = 1;
+            sd->dp_tries = 0;
+        } else {
+            sd->dp_accept = 0;
+            sd->dp_rejects += 1;
+            sd->dp_tries += 1;
+            if (sd->dp_tries >= kDpMaxTry || !(sd->dt > 0.0)) sd->status = kStatusDpFail;
+        }
+    }
+}
+
+// accepted DP5CN attempt: the trial solution (ACC) becomes the state (U);
+// only the dealiased sphere is copied. grid (x, members)
+template <typename T, int N>
+__global__ void k_dp_commit(cx<T>* __restrict__ U, const cx<T>* __restrict__ ACC, const StepDev* __restrict__ sd) {
+    using G = Geo<N>;
+    const long long mem = blockIdx.y;
+    if (!sd[mem].dp_accept) return;
+    U += mem * 3 * G::FS;
+    ACC += mem * 3 * G::FS;
+    const long long n = (long long)N * N * G::NZP;
+    for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+        const int kz = (int)(q % G::NZP);
+        const long long ij = q / G::NZP;
+        const int kx = kof<N>((int)(ij / N)), ky = kof<N>((int)(ij % N));
+        if (kz > G::KC || kx * kx + ky * ky + kz * kz > G::KC2) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) U[c * G::FS + q] = ACC[c * G::FS + q];
     }
 }
 

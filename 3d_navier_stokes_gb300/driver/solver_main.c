@@ -39,7 +39,7 @@ typedef struct {
 
 static void usage_exit(void) {
     fprintf(stderr, "Use -o output dir, -n N (x3), -s t0, -e T, -h dt, -c CFL, -v nu, -i IC, -t tag, -f forcing,\n"
-                    "    -p save every, -z checkpoint; -I ifrk4|rk4cn, -P fp64|fp32, -H, -a, -S seed, -k k0,\n"
+                    "    -p save every, -z checkpoint; -I ifrk4|rk4cn|rk5cn|dp5cn, -P fp64|fp32, -H, -a, -S seed, -k k0,\n"
                     "    -E energy, -F force_k, -R, -x\n"
                     "Example: ./solver -o ../Data/Tmp -n 64 -n 64 -n 64 -s 0.0 -e 1.0 -h 0.001 -v 0.0025 -i TAYLOR_GREEN\n");
     exit(1);
@@ -131,7 +131,12 @@ static void parse(int argc, char** argv, opts_t* o) {
                     exit(1);
                 }
                 break;
-            case 'I': o->integ = !strcmp(optarg, "rk4cn") ? NS3D_RK4CN : NS3D_IFRK4; break;
+            case 'I':
+                o->integ = !strcmp(optarg, "rk4cn")   ? NS3D_RK4CN
+                           : !strcmp(optarg, "rk5cn") ? NS3D_RK5CN
+                           : !strcmp(optarg, "dp5cn") ? NS3D_DP5CN
+                                                      : NS3D_IFRK4;
+                break;
             case 'P': o->prec = !strcmp(optarg, "fp32") ? NS3D_FP32 : NS3D_FP64; break;
             case 'H': o->hyper = 1; break;
             case 'a': o->adaptive = 1; break;
@@ -330,7 +335,7 @@ int main(int argc, char** argv) {
     p.visc_pow = o.hyper ? 2 : 1;
     p.integrator = o.integ;
     p.precision = o.prec;
-    p.cfl = o.adaptive ? o.cfl : 0.0;
+    p.cfl = (o.adaptive && o.integ != NS3D_DP5CN) ? o.cfl : 0.0;   /* DP5CN controls its own step */
     p.forcing = !strcmp(o.forcing, "SHELL") ? NS3D_FORCE_SHELL : NS3D_FORCE_NONE;
     p.force_k = o.force_k;
     ns3d_ctx* ctx = NULL;
@@ -359,7 +364,8 @@ int main(int argc, char** argv) {
     mkdir_or_die(o.output_dir);
     snprintf(dir, sizeof(dir), "%s", o.output_dir);
     if (dir[strlen(dir) - 1] != '/') strcat(dir, "/");
-    const char* solv = o.integ == NS3D_RK4CN ? "RK4" : "IFRK4";
+    /* solver-type tag of GetOutputDirPath (hdf5_funcs.c:372-380) */
+    const char* solv = o.integ == NS3D_RK4CN ? "RK4" : o.integ == NS3D_RK5CN ? "RK5" : o.integ == NS3D_DP5CN ? "DP5" : "IFRK4";
     if (o.file_only) {
         char fd[512];
         snprintf(fd, sizeof(fd), "_SIM[NAV-%s-FULL]_N[%d,%d]_T[%d-%d]_NU[%1.10lf]_CFL[%1.2lf]_u0[%s]", solv, N, N,
@@ -395,11 +401,11 @@ int main(int argc, char** argv) {
     record(&R, iters0);
     /* the time loop (solver.c:125-194): t = t0 + iters * dt while t <= T */
     long iters = iters0;
-    if (p.cfl > 0) {
+    if (p.cfl > 0 || p.integrator == NS3D_DP5CN) {
         for (;;) {
             check(ctx, ns3d_get_time(ctx, &t, &dt, &iters), "ns3d_get_time");
             if (t + dt > o.T + 1e-12 * o.T) break;
-            check(ctx, ns3d_step(ctx, 1), "RK4Step");
+            check(ctx, ns3d_step(ctx, 1), p.integrator >= NS3D_RK5CN ? "RK5DPStep" : "RK4Step");
             if ((iters + 1) % o.save_every == 0) record(&R, iters + 1);
         }
     } else {

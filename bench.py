@@ -45,7 +45,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble"])
+    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256"])
+    ap.add_argument("--snapshots", type=int, default=200)
+    ap.add_argument("--train-iters", type=int, default=2000)
+    ap.add_argument("--les-steps", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -350,6 +353,102 @@ def run_ensemble(args, local):
     ens.close()
 
 
+def run_les(args, local):
+    """Config C5: snapshots of a seeded forced 256^3 FP32 DNS box-filtered to 64^3 train the closure
+    network on the GPU; a 64^3 run with the closure and the plain 64^3 solve then start from the filtered
+    DNS and are compared with it after the same number of steps (E(k) log error over k = 1..21), with
+    their speeds. --snapshots, --train-iters and --les-steps set the sizes."""
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    Nf, Nc, nu, dt = 256, 64, 1.5e-3, 1e-3
+    dns = pkg.Solver(Nf, nu=nu, dt=dt, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    dns.InitialConditions("SPECTRUM", seed=0, k0=3.0)
+    dns.RK4Step(500)
+    les = pkg.LES(Nc, capacity=args.snapshots, seed=0)
+    t0 = time.perf_counter()
+    for _ in range(args.snapshots):
+        dns.RK4Step(5)
+        les.add_snapshot(dns)
+    t_data = time.perf_counter() - t0
+    loss0 = les.dataset_loss()
+    t0 = time.perf_counter()
+    loss_tr = les.train(args.train_iters, lr=1e-3)
+    t_train = time.perf_counter() - t0
+    loss1 = les.dataset_loss()
+    ubar = les.filtered_velocity(dns)
+    runs = {}
+    for name in ("closure", "plain"):
+        c = pkg.Solver(Nc, nu=nu, dt=dt, precision="fp32", forcing="SHELL", force_k=2, device=local)
+        c.set_state_real(ubar)
+        if name == "closure":
+            c.attach_closure(les)
+        runs[name] = c
+    ms = {}
+    dns.RK4Step(args.les_steps)
+    ms["dns"] = dns.last_step_ms() / args.les_steps
+    for n, c in runs.items():
+        c.RK4Step(args.les_steps)
+        ms[n] = c.last_step_ms() / args.les_steps
+    ref = pkg.Solver(Nc, nu=nu, dt=dt, precision="fp32", device=local)
+    ref.set_state_real(les.filtered_velocity(dns))
+    _, Eref, _ = ref.ComputeSystemMeasurables()
+    k = np.arange(1, Nc // 3 + 1)
+    err = {}
+    for n, c in runs.items():
+        _, E, _ = c.ComputeSystemMeasurables()
+        err[n] = float(np.sqrt(np.mean((np.log(E[k]) - np.log(Eref[k])) ** 2)))
+    on, off = runs["closure"].closure_counters()
+    line = {"metric": "LES E(k) log-error vs filtered 256^3 DNS (64^3, closure vs plain)",
+            "value": err["closure"], "unit": "rms log E(k) error", "higher_is_better": False,
+            "plain_coarse_error": err["plain"], "n_gpus": 1, "steps": args.les_steps, "dtype": "f32 (bf16 weights)",
+            "data": "synthetic", "config": {"workload": "learned closure C5", "dns_N": Nf, "les_N": Nc, "nu": nu,
+                                            "dt": dt, "snapshots": args.snapshots, "train_iters": args.train_iters},
+            "ms_per_step": {"dns_256": ms["dns"], "les_64_closure": ms["closure"], "plain_64": ms["plain"]},
+            "speedup_vs_dns": ms["dns"] / ms["closure"], "closure_steps": on, "fallback_steps": off,
+            "loss": {"before": loss0, "after": loss1, "train_tail": loss_tr},
+            "seconds": {"data": t_data, "train": t_train}}
+    print(json.dumps(line), flush=True)
+    les.close()
+
+
+def run_decay(args, local):
+    """Config C2: decaying turbulence at 256^3 (SPECTRUM IC k0 = 4, nu = 2e-3, CFL 0.5, IF-RK4,
+    --les-steps steps) in FP64 and in FP32; reports the FP32 relative errors of the energy, the
+    dissipation and E(k) against FP64, and both step rates."""
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    N, steps = 256, args.les_steps
+    res = {}
+    for prec in ("fp64", "fp32"):
+        s = pkg.Solver(N, nu=2e-3, dt=1e-3, cfl=0.5, precision=prec, device=local)
+        s.InitialConditions("SPECTRUM", seed=0, k0=4.0)
+        s.RK4Step(steps)
+        tot, Ek, _ = s.ComputeSystemMeasurables()
+        res[prec] = (tot, Ek, s.last_step_ms() / steps, s.get_time())
+        s.close()
+    t64, t32 = res["fp64"][0], res["fp32"][0]
+    E64, E32 = res["fp64"][1], res["fp32"][1]
+    kk = np.arange(1, N // 3 + 1)
+    line = {"metric": "FP32 vs FP64 relative energy error, 256^3 decaying turbulence",
+            "value": abs(t32["energy"] - t64["energy"]) / t64["energy"], "unit": "relative error",
+            "higher_is_better": False, "steps": steps, "n_gpus": 1, "data": "synthetic", "dtype": "f32 vs f64",
+            "dissipation_rel_err": abs(t32["dissipation"] - t64["dissipation"]) / t64["dissipation"],
+            "Ek_max_rel_err_k1_to_85": float(np.max(np.abs(E32[kk] - E64[kk]) / E64[kk])),
+            "ms_per_step": {"fp64": res["fp64"][2], "fp32": res["fp32"][2]},
+            "fp32_over_fp64_speed": res["fp64"][2] / res["fp32"][2],
+            "t_final": {"fp64": res["fp64"][3][0], "fp32": res["fp32"][3][0]},
+            "config": {"workload": "decaying turbulence C2", "N": N, "nu": 2e-3, "cfl": 0.5, "k0": 4.0}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -358,6 +457,12 @@ def main():
         return
     if args.workload == "ensemble":
         run_ensemble(args, local)
+        return
+    if args.workload == "les":
+        run_les(args, local)
+        return
+    if args.workload == "decay256":
+        run_decay(args, local)
         return
     run_ours(args, ws, rank, local)
 

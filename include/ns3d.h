@@ -37,7 +37,12 @@ typedef enum {
 } ns3d_status;
 
 typedef enum { NS3D_FP64 = 0, NS3D_FP32 = 1 } ns3d_precision;
-typedef enum { NS3D_IFRK4 = 0, NS3D_RK4CN = 1 } ns3d_integrator;
+/* IFRK4: integrating-factor RK4 (Lawson). RK4CN: the reference's RK4Step
+ * (solver.c:505-608). RK5CN: its RK5DPStep built with __RK5 (solver.c:217-421),
+ * fixed step. DP5CN: its adaptive Dormand-Prince loop (__DPRK5, solver.c:
+ * 134-154), single runs only, cfl must be 0. Both RK5 variants use the
+ * published Dormand-Prince table (a32 = 9/40; the reference has 1/2). */
+typedef enum { NS3D_IFRK4 = 0, NS3D_RK4CN = 1, NS3D_RK5CN = 2, NS3D_DP5CN = 3 } ns3d_integrator;
 typedef enum { NS3D_FORCE_NONE = 0, NS3D_FORCE_SHELL = 1 } ns3d_forcing;
 
 /* Parameters: the hot-path fields of system_vars_struct (data_types.h:147-185)
@@ -48,7 +53,7 @@ typedef struct {
     double dt;          /* time step (sys_vars->dt); initial step when cfl > 0          */
     double t0;          /* start time (sys_vars->t0)                                    */
     int    visc_pow;    /* 1: nu k^2; 2: nu k^4 (HYPER_VISC, VIS_POW, data_types.h:68-71) */
-    int    integrator;  /* ns3d_integrator; RK4CN is the reference's RK4Step          */
+    int    integrator;  /* ns3d_integrator; RK4CN is the reference's RK4Step           */
     int    precision;   /* ns3d_precision: FP64, or FP32 bulk with FP64 integrating
                            factors, time accumulator and reductions                   */
     double cfl;         /* > 0: dt = cfl * dx / max(|u|+|v|+|w|) every step (CFL_CONST)  */
@@ -141,6 +146,14 @@ ns3d_status ns3d_set_time(ns3d_ctx* ctx, double t, double dt, long iters);
 /* Forcing target energy (set by initial conditions / set_state). */
 ns3d_status ns3d_get_forcing_target(ns3d_ctx* ctx, double* e);
 ns3d_status ns3d_set_forcing_target(ns3d_ctx* ctx, double e);
+
+/* DP5CN step control: error tolerances (default 1e-7 / 1e-7, DP_ABS_TOL and
+ * DP_REL_TOL of data_types.h:123-124), and the error norm of the last attempt
+ * with the number of rejected attempts so far. With DP5CN, ns3d_step(ctx, n)
+ * returns after n accepted steps; n steps rejected DP_MAX_TRY = 50 times in a
+ * row end it with NS3D_ERR_NUMERIC. */
+ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* ctx, double atol, double rtol);
+ns3d_status ns3d_dp_stats(ns3d_ctx* ctx, double* last_err, long* rejects);
 
 /* Largest |u|+|v|+|w| over the grid for the current state (CFL numerator). */
 ns3d_status ns3d_max_speed_sum(ns3d_ctx* ctx, double* umax);

@@ -43,7 +43,8 @@ typedef struct system_vars_struct {
     int SAVE_EVERY;
     /* switches that the reference sets at compile time (Makefile:43-53) */
     int hyper_visc;        /* 1: nu k^4 (HYPER_VISC, VIS_POW 2.0)             */
-    int integrator;        /* 0: IF-RK4, 1: RK4 + Crank-Nicolson (RK4Step)      */
+    int integrator;        /* 0: IF-RK4, 1: RK4 + Crank-Nicolson (RK4Step),
+                              2: RK5 (__RK5), 3: Dormand-Prince (__DPRK5)      */
     int precision;         /* 0: FP64, 1: FP32 bulk                          */
     int adaptive_step;     /* 1: CFL step (__ADAPTIVE_STEP)                   */
 } system_vars_struct;
@@ -80,6 +81,8 @@ void InitializeSpaceVariables(double** x, int** k, const long int* N);
 void InitialConditions(ns3d_fftw_complex* u_hat, double* u, const long int* N);
 /* solver.c:505-608: one step of run_data->u_hat in place */
 void RK4Step(const double dt, const long int* N, const ptrdiff_t local_Nx, RK_data_struct* RK_data);
+/* solver.c:217-421 (integrator 2 or 3; for 3 one accepted adaptive step) */
+void RK5DPStep(const double dt, const long int* N, const int iters, const ptrdiff_t local_Nx, RK_data_struct* RK_data);
 /* solver.c:620-731 (curl, u, vort are the reference's scratch; unused here) */
 void NonlinearRHSBatch(ns3d_fftw_complex* u_hat, ns3d_fftw_complex* dw_hat_dt, double* curl, double* u,
                        double* vort);

@@ -25,6 +25,8 @@
  *       zero: fixed to Re(u.conj(w)); bugcompat_measures keeps the old form.
  *   D13 SHAPIRO w = A cos cos cos(Mz) (solver.c:1593, 1686) is not divergence
  *       free: fixed to sin(Mz); bugcompat_measures keeps the old form.
+ *   D15-D19 in the RK5 / Dormand-Prince stepper (solver.c:34-42, 85-154,
+ *       217-421): see the comment above rk5_attempt.
  *
  * c2r semantics (FFTW's, restated): the two complex axes are inverted as full
  * complex transforms, then each z line is extended by Hermitian symmetry and
@@ -165,7 +167,10 @@ struct orc_ctx {
     fft_plan plan;
     cplx* u_hat;             /* state, reference layout */
     cplx *rk1, *rk2, *rk3, *rk4, *rk_tmp, *w_hat;
+    cplx *rk5, *rk6, *rk7, *u_new;   /* RK5CN / DP5CN only */
     double *vel, *vort, *curl;
+    double dp_err;           /* DP5CN: error norm of the last attempt */
+    long dp_rejects;
     double t, dt;
     long iters;
     double force_target;
@@ -222,6 +227,14 @@ orc_ctx* orc_create(const orc_params* p) {
     c->rk4 = (cplx*)calloc(1, fb);
     c->rk_tmp = (cplx*)calloc(1, fb);
     c->w_hat = (cplx*)calloc(1, fb);
+    if (p->integrator == ORC_RK5CN || p->integrator == ORC_DP5CN) {
+        c->rk5 = (cplx*)calloc(1, fb);
+        c->rk6 = (cplx*)calloc(1, fb);
+        c->rk7 = (cplx*)calloc(1, fb);
+        c->u_new = (cplx*)calloc(1, fb);
+    }
+    if (!(c->p.dp_atol > 0.0)) c->p.dp_atol = 1e-7;
+    if (!(c->p.dp_rtol > 0.0)) c->p.dp_rtol = 1e-7;
     c->vel = (double*)calloc(1, rb);
     c->vort = (double*)calloc(1, rb);
     c->curl = (double*)calloc(1, rb);
@@ -237,6 +250,7 @@ void orc_destroy(orc_ctx* c) {
     plan_free(&c->plan);
     free(c->u_hat); free(c->rk1); free(c->rk2); free(c->rk3); free(c->rk4);
     free(c->rk_tmp); free(c->w_hat); free(c->vel); free(c->vort); free(c->curl);
+    free(c->rk5); free(c->rk6); free(c->rk7); free(c->u_new);
     free(c);
 }
 
@@ -566,8 +580,153 @@ static void one_step(orc_ctx* c) {
     else c->t = c->p.t0 + (double)c->iters * h;
 }
 
-void orc_step(orc_ctx* c, int nsteps) {
-    for (int s = 0; s < nsteps; ++s) one_step(c);
+/* ------------------------------------------------------------------------ */
+/* RK5 family: RK5DPStep (solver.c:217-421) with the Crank–Nicolson factor   */
+/* of the __NAVIER branch (solver.c:356-371), and the adaptive Dormand–      */
+/* Prince loop of SpectralSolve (solver.c:134-154).                          */
+/*   stages   k_s = N(u + h sum_{j<s} a_sj k_j)      (no viscosity in stages) */
+/*   update   u+ = u (2-D)/(2+D) + 2h/(2+D) sum_j b_j k_j,  D = h nu k^2p     */
+/* RK5CN evaluates 6 stages; DP5CN a 7th (a_7j = b_j) for the embedded        */
+/* 4th-order solution u* = u (2-D)/(2+D) + 2h/(2+D) sum_j b*_j k_j and        */
+/*   err = max_d sqrt( sum_modes |u+_d - u*_d|^2 / den_d^2 / (N N (N/2+1)) ), */
+/*   den_d = atol + max(|u_d|, |u+_d|) rtol   (solver.c:382-408)             */
+/* The step is accepted when err <= 1; either way the next attempt uses      */
+/*   h' = h min(1.5, max(0.01, 0.8 err^(-1/5)))   (solver.c:140).            */
+/* Defects of the reference fixed here:                                       */
+/*   D15 the accept test is inverted (a step with err <= 1 is retried,        */
+/*       solver.c:143) and a rejected attempt is not undone (the next attempt */
+/*       starts from the already updated u_hat): here err <= 1 accepts and a  */
+/*       rejection restarts from the step's initial state.                    */
+/*   D16 err_sum_* are used uninitialised (solver.c:229-232) and no error is  */
+/*       formed on the first step (iters > 1, solver.c:374): here the sums    */
+/*       start at 0 on every attempt.                                         */
+/*   D17 the higher-order solution is built from the updated u_hat without    */
+/*       the viscous factor (solver.c:376-378), so the "error" is            */
+/*       dt sum b*_j k_j, not a difference of two solutions: here u+ - u*.    */
+/*   D18 pow() of a complex argument keeps only its real part                 */
+/*       (solver.c:387-389): here |.|^2 of the complex difference; the retry  */
+/*       counter is never reset (solver.c:91): here 50 tries per step; t is   */
+/*       iters*dt with a variable dt (solver.c:193): here t += h.             */
+/*   D19 a32 = 1/2 (solver.c:36); Dormand & Prince (1980) have 9/40, which    */
+/*       the consistency condition a31 + a32 = c3 = 3/10 requires.           */
+/*       bugcompat_rk5 keeps 1/2.                                             */
+/* ------------------------------------------------------------------------ */
+static const double DP_A[7][6] = {
+    {0, 0, 0, 0, 0, 0},
+    {1.0 / 5.0, 0, 0, 0, 0, 0},
+    {3.0 / 40.0, 9.0 / 40.0, 0, 0, 0, 0},
+    {44.0 / 45.0, -56.0 / 15.0, 32.0 / 9.0, 0, 0, 0},
+    {19372.0 / 6561.0, -25360.0 / 2187.0, 64448.0 / 6561.0, -212.0 / 729.0, 0, 0},
+    {9017.0 / 3168.0, -355.0 / 33.0, 46732.0 / 5247.0, 49.0 / 176.0, -5103.0 / 18656.0, 0},
+    {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0}};
+static const double DP_B[7] = {35.0 / 384.0, 0, 500.0 / 1113.0, 125.0 / 192.0, -2187.0 / 6784.0, 11.0 / 84.0, 0};
+static const double DP_BS[7] = {5179.0 / 57600.0, 0, 7571.0 / 16695.0, 393.0 / 640.0, -92097.0 / 339200.0,
+                                187.0 / 2100.0, 1.0 / 40.0};
+
+/* one RK5CN step (dp = 0, written into u_hat) or one DP5CN attempt (dp = 1,
+   written into u_new; returns the error norm) */
+static double rk5_attempt(orc_ctx* c, double h, int dp) {
+    const int N = c->N, NF = c->NF;
+    cplx* u = c->u_hat;
+    cplx* K[7] = {c->rk1, c->rk2, c->rk3, c->rk4, c->rk5, c->rk6, c->rk7};
+    const int S = dp ? 7 : 6;
+    double A[7][6];
+    memcpy(A, DP_A, sizeof(A));
+    if (c->p.bugcompat_rk5) A[2][1] = 0.5;
+    rhs_impl(c, u, K[0], 0);
+    for (int s = 1; s < S; ++s) {
+        FOR_MODES {
+            long x = 3 * ((long)(i * N + j) * NF + k);
+            for (int d = 0; d < 3; ++d) {
+                cplx v = u[x + d];
+                for (int q = 0; q < s; ++q) v += h * A[s][q] * K[q][x + d];
+                c->rk_tmp[x + d] = v;
+            }
+        }
+        rhs_impl(c, c->rk_tmp, K[s], 0);
+    }
+    cplx* out = dp ? c->u_new : u;
+    const double atol = c->p.dp_atol, rtol = c->p.dp_rtol;
+    double e0 = 0.0, e1 = 0.0, e2 = 0.0;
+#pragma omp parallel for collapse(2) schedule(static) reduction(+ : e0, e1, e2)
+    for (int i = 0; i < N; ++i)
+        for (int j = 0; j < N; ++j)
+            for (int k = 0; k < NF; ++k) {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double D = h * visc(c, i, j, k);
+                double a = (2.0 - D) / (2.0 + D), b = 2.0 * h / (2.0 + D);
+                for (int d = 0; d < 3; ++d) {
+                    cplx sb = 0.0, se = 0.0;
+                    for (int q = 0; q < 6; ++q) sb += DP_B[q] * K[q][x + d];
+                    cplx un = u[x + d] * a + b * sb;
+                    if (dp) {
+                        for (int q = 0; q < 7; ++q) se += (DP_B[q] - DP_BS[q]) * K[q][x + d];
+                        cplx diff = b * se;
+                        double m0 = cabs(u[x + d]), m1 = cabs(un);
+                        double den = atol + (m0 > m1 ? m0 : m1) * rtol;
+                        double r = (creal(diff) * creal(diff) + cimag(diff) * cimag(diff)) / (den * den);
+                        if (d == 0) e0 += r; else if (d == 1) e1 += r; else e2 += r;
+                    }
+                    out[x + d] = un;
+                }
+            }
+    if (!dp) return 0.0;
+    const double nm = (double)N * N * NF;
+    double err = sqrt(e0 / nm);
+    if (sqrt(e1 / nm) > err) err = sqrt(e1 / nm);
+    if (sqrt(e2 / nm) > err) err = sqrt(e2 / nm);
+    return err;
+}
+
+static void end_step(orc_ctx* c, double h, int var_dt) {
+    if (c->p.forcing == ORC_FORCE_SHELL) apply_forcing(c);
+    c->iters += 1;
+    if (var_dt) c->t += h;
+    else c->t = c->p.t0 + (double)c->iters * h;
+}
+
+static int rk5_step(orc_ctx* c) {
+    const int N = c->N;
+    if (c->p.integrator == ORC_RK5CN) {
+        const int cfl = c->p.cfl > 0.0;
+        if (cfl) {
+            rhs_impl(c, c->u_hat, c->rk1, 1);
+            if (c->last_umax > 0.0) c->dt = c->p.cfl * (2.0 * M_PI / (double)N) / c->last_umax;
+        }
+        rk5_attempt(c, c->dt, 0);
+        end_step(c, c->dt, cfl);
+        return 0;
+    }
+    for (int tries = 0; tries < 50; ++tries) {
+        const double h = c->dt;
+        const double err = rk5_attempt(c, h, 1);
+        double fac = 0.8 * pow(1.0 / err, 0.2);
+        fac = fac < 0.01 ? 0.01 : fac;
+        fac = fac > 1.5 ? 1.5 : fac;
+        c->dp_err = err;
+        c->dt = h * fac;
+        if (err <= 1.0) {
+            memcpy(c->u_hat, c->u_new, sizeof(cplx) * 3 * (size_t)c->nF);
+            end_step(c, h, 1);
+            return 0;
+        }
+        c->dp_rejects++;
+    }
+    return 1;
+}
+
+void orc_dp_stats(const orc_ctx* c, double* last_err, long* rejects) {
+    if (last_err) *last_err = c->dp_err;
+    if (rejects) *rejects = c->dp_rejects;
+}
+
+int orc_step(orc_ctx* c, int nsteps) {
+    const int rk5 = c->p.integrator == ORC_RK5CN || c->p.integrator == ORC_DP5CN;
+    for (int s = 0; s < nsteps; ++s) {
+        if (!rk5) one_step(c);
+        else if (rk5_step(c)) return 1;
+    }
+    return 0;
 }
 
 /* ------------------------------------------------------------------------ */

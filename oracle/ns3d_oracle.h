@@ -21,7 +21,7 @@ extern "C" {
 
 typedef struct orc_ctx orc_ctx;
 
-enum { ORC_IFRK4 = 0, ORC_RK4CN = 1 };
+enum { ORC_IFRK4 = 0, ORC_RK4CN = 1, ORC_RK5CN = 2, ORC_DP5CN = 3 };
 enum { ORC_FORCE_NONE = 0, ORC_FORCE_SHELL = 1 };
 
 typedef struct {
@@ -30,13 +30,15 @@ typedef struct {
     double dt;                 /* time step (initial step when cfl > 0)             */
     double t0;                 /* start time                                        */
     int    visc_pow;           /* 1: nu k^2, 2: nu k^4 (reference HYPER_VISC)       */
-    int    integrator;         /* ORC_IFRK4 or ORC_RK4CN                            */
+    int    integrator;         /* ORC_IFRK4, ORC_RK4CN, ORC_RK5CN or ORC_DP5CN       */
     double cfl;                /* > 0: dt = cfl*dx/max(|u|+|v|+|w|) every step      */
     int    forcing;            /* ORC_FORCE_NONE / ORC_FORCE_SHELL                  */
     int    force_k;            /* shells round(|k|) <= force_k held at fixed energy */
     int    bugcompat_dealias;  /* reproduce defect D2 (solver.c:1741)               */
     int    bugcompat_measures; /* reproduce defect D4 (solver.c:1232-1235)          */
     int    nthreads;           /* OpenMP threads (<= 0: runtime default)            */
+    int    bugcompat_rk5;      /* reproduce defect D19: a32 = 1/2 (solver.c:36)      */
+    double dp_atol, dp_rtol;   /* DP5CN error tolerances (<= 0: 1e-7, data_types.h:123-124) */
 } orc_params;
 
 orc_ctx* orc_create(const orc_params* p);
@@ -58,7 +60,10 @@ void orc_fft1d(int n, const double* in, double* out, int inverse);
 
 void orc_dealias(orc_ctx* c, double* arr, int array_dim);
 void orc_rhs(orc_ctx* c, const double* u_hat, double* rhs);
-void orc_step(orc_ctx* c, int nsteps);
+/* returns 0, or 1 when a DP5CN step was rejected DP_MAX_TRY = 50 times in a row */
+int  orc_step(orc_ctx* c, int nsteps);
+/* DP5CN: error norm of the last attempt, rejected attempts so far */
+void orc_dp_stats(const orc_ctx* c, double* last_err, long* rejects);
 void orc_measurables(orc_ctx* c, double* totals5, double* Ek, double* Ok);
 int  orc_ic(orc_ctx* c, const char* name, uint64_t seed, double k0, double energy);
 void orc_real_space(orc_ctx* c, double* u, double* w);

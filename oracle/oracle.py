@@ -20,7 +20,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "libns3d_oracle.so")
 _lib = None
 
-IFRK4, RK4CN = 0, 1
+IFRK4, RK4CN, RK5CN, DP5CN = 0, 1, 2, 3
 FORCE_NONE, FORCE_SHELL = 0, 1
 
 
@@ -38,6 +38,9 @@ class _Params(ctypes.Structure):
         ("bugcompat_dealias", ctypes.c_int),
         ("bugcompat_measures", ctypes.c_int),
         ("nthreads", ctypes.c_int),
+        ("bugcompat_rk5", ctypes.c_int),
+        ("dp_atol", ctypes.c_double),
+        ("dp_rtol", ctypes.c_double),
     ]
 
 
@@ -74,6 +77,8 @@ def lib():
         L.orc_dealias.argtypes = [P, D, ctypes.c_int]
         L.orc_rhs.argtypes = [P, D, D]
         L.orc_step.argtypes = [P, ctypes.c_int]
+        L.orc_step.restype = ctypes.c_int
+        L.orc_dp_stats.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_measurables.argtypes = [P, D, D, D]
         L.orc_ic.restype = ctypes.c_int
         L.orc_ic.argtypes = [P, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_double]
@@ -109,10 +114,10 @@ class Oracle:
 
     def __init__(self, N, nu=1.0, dt=1e-3, t0=0.0, visc_pow=1, integrator=IFRK4, cfl=0.0,
                  forcing=FORCE_NONE, force_k=2, bugcompat_dealias=False,
-                 bugcompat_measures=False, nthreads=0):
+                 bugcompat_measures=False, nthreads=0, bugcompat_rk5=False, dp_atol=0.0, dp_rtol=0.0):
         self.N = N
         p = _Params(N, nu, dt, t0, visc_pow, integrator, cfl, forcing, force_k,
-                    int(bugcompat_dealias), int(bugcompat_measures), nthreads)
+                    int(bugcompat_dealias), int(bugcompat_measures), nthreads, int(bugcompat_rk5), dp_atol, dp_rtol)
         self._c = lib().orc_create(ctypes.byref(p))
         if not self._c:
             raise ValueError(f"oracle rejected N={N}")
@@ -182,7 +187,14 @@ class Oracle:
         return out
 
     def step(self, n=1):
-        lib().orc_step(self._c, n)
+        if lib().orc_step(self._c, n) != 0:
+            raise RuntimeError("DP5CN step rejected 50 times in a row")
+
+    def dp_stats(self):
+        """(error norm of the last DP5CN attempt, rejected attempts so far)"""
+        e, r = ctypes.c_double(), ctypes.c_long()
+        lib().orc_dp_stats(self._c, ctypes.byref(e), ctypes.byref(r))
+        return e.value, r.value
 
     def measurables(self):
         ns = n_spect(self.N)

@@ -93,6 +93,45 @@ def step_rk4cn(uh, N, nu, h, vp=1):
     return uh * ((2 - D) / (2 + D)) + (2 * h / (2 + D)) * (k1 / 6 + k2 / 3 + k3 / 3 + k4 / 6)
 
 
+# Dormand & Prince (1980) RK5(4)7M; the reference's table (solver.c:34-42)
+# has a32 = 1/2 where the published scheme has 9/40 (defect D19, fixed)
+DP_A = [[], [1 / 5], [3 / 40, 9 / 40], [44 / 45, -56 / 15, 32 / 9],
+        [19372 / 6561, -25360 / 2187, 64448 / 6561, -212 / 729],
+        [9017 / 3168, -355 / 33, 46732 / 5247, 49 / 176, -5103 / 18656],
+        [35 / 384, 0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84]]
+DP_B = [35 / 384, 0, 500 / 1113, 125 / 192, -2187 / 6784, 11 / 84, 0]
+DP_BS = [5179 / 57600, 0, 7571 / 16695, 393 / 640, -92097 / 339200, 187 / 2100, 1 / 40]
+
+
+def rk5_attempt(uh, N, nu, h, dp, vp=1, atol=1e-7, rtol=1e-7):
+    # RK5DPStep, solver.c:217-421: explicit stages on N(u), Crank–Nicolson
+    # factor in the update; dp adds the 7th stage and the embedded error
+    D = h * visc(N, nu, vp)
+    ks = [rhs(uh, N)]
+    for s in range(1, 7 if dp else 6):
+        ks.append(rhs(uh + h * sum(a * k for a, k in zip(DP_A[s], ks)), N))
+    a, b = (2 - D) / (2 + D), 2 * h / (2 + D)
+    un = uh * a + b * sum(c * k for c, k in zip(DP_B, ks))
+    if not dp:
+        return un, None
+    diff = b * sum((c - cs) * k for c, cs, k in zip(DP_B, DP_BS, ks))
+    den = atol + np.maximum(np.abs(uh), np.abs(un)) * rtol
+    err = np.sqrt(np.sum(np.abs(diff / den) ** 2, axis=(0, 1, 2)) / (N * N * (N // 2 + 1))).max()
+    return un, err
+
+
+def dp5_step(uh, N, nu, h):
+    # adaptive loop (solver.c:134-154, D15/D18 fixed): retry from uh until err <= 1
+    rejects = 0
+    while True:
+        un, err = rk5_attempt(uh, N, nu, h, True)
+        hn = h * min(1.5, max(0.01, 0.8 * (1.0 / err) ** 0.2))
+        if err <= 1.0:
+            return un, h, hn, err, rejects
+        rejects += 1
+        h = hn
+
+
 def measurables(uh, N, nu, vp=1):
     # ComputeSystemMeasurables, solver.c:1142-1276 (D4 fixed)
     KX, KY, KZ = wavenumbers(N)
@@ -134,6 +173,10 @@ def make(N, nu=0.05, h=1e-2, seed=1234):
     out["ifrk4_10"] = u
     out["rk4cn_1"] = step_rk4cn(u0, N, nu, h)
     out["ifrk4_hyper_1"] = step_ifrk4(u0, N, nu * 1e-2, h, vp=2)
+    out["rk5cn_1"] = rk5_attempt(u0, N, nu, h, False)[0]
+    # a first step 30x too long: rejected, then accepted with a shorter step
+    un, h_used, h_next, err, rej = dp5_step(u0, N, nu, 30 * h)
+    out.update(dp5_1=un, dp5_h_used=h_used, dp5_h_next=h_next, dp5_err=err, dp5_rejects=rej)
     tot, Ek, Ok = measurables(u0, N, nu)
     out.update(tot=tot, Ek=Ek, Ok=Ok)
     return out

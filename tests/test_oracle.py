@@ -183,3 +183,65 @@ def test_cfl_step(oracle):
     o.step(1)
     t, dt, it = o.get_time()
     assert it == 1 and abs(dt - cfl * (2 * np.pi / N) / umax) < 1e-12 * dt and abs(t - dt) < 1e-15
+
+
+@pytest.mark.parametrize("N", [8, 12])
+def test_oracle_rk5_vs_numpy_golden(oracle, N):
+    d = np.load(os.path.join(GOLD, f"golden_N{N}.npz"))
+    nu, dt = float(d["nu"]), float(d["dt"])
+    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=oracle.RK5CN)
+    o.set_state(d["u0"]); o.step(1)
+    assert rel(o.get_state(), d["rk5cn_1"]) < 1e-13
+    dp = oracle.Oracle(N, nu=nu, dt=30 * dt, integrator=oracle.DP5CN)
+    dp.set_state(d["u0"]); dp.step(1)
+    assert rel(dp.get_state(), d["dp5_1"]) < 1e-13
+    err, rejects = dp.dp_stats()
+    t, h_next, iters = dp.get_time()
+    assert rejects == int(d["dp5_rejects"]) and iters == 1
+    # the error norm is a difference of two solutions: relative agreement ~1e-10
+    assert abs(err - float(d["dp5_err"])) < 1e-9 * float(d["dp5_err"])
+    # step sizes follow err^(-1/5)
+    assert abs(t / float(d["dp5_h_used"]) - 1) < 1e-10 and abs(h_next / float(d["dp5_h_next"]) - 1) < 1e-10
+
+
+def _order_runs(oracle, integrator, bugcompat=False):
+    # nu = 0: the Crank–Nicolson factor is 1 and the stepper is the plain explicit scheme
+    N = 12
+    d = np.load(os.path.join(GOLD, "golden_N12.npz"))
+    u0 = d["u0"] / np.abs(d["u0"]).max() * 200.0
+    T = 0.08
+
+    def run(h):
+        o = oracle.Oracle(N, nu=0.0, dt=h, integrator=integrator, bugcompat_rk5=bugcompat)
+        o.set_state(u0)
+        o.step(int(round(T / h)))
+        return o.get_state()
+
+    ref = run(T / 64)
+    return np.abs(run(T / 4) - ref).max() / np.abs(run(T / 8) - ref).max()
+
+
+def test_rk5cn_fifth_order(oracle):
+    # published tableau: 2^5 = 32; the reference's a32 = 1/2 (D19) loses consistency
+    assert 25 < _order_runs(oracle, oracle.RK5CN) < 40
+    assert _order_runs(oracle, oracle.RK5CN, bugcompat=True) < 5
+
+
+def test_dp5_adaptive_control(oracle):
+    # step-size control on a Taylor–Green run: the error of every accepted step
+    # is <= 1, steps grow by at most 1.5x and a too-long first step is rejected
+    o = oracle.Oracle(16, nu=0.01, dt=0.5, integrator=oracle.DP5CN, dp_atol=1e-9, dp_rtol=1e-9)
+    o.ic("TAYLOR_GREEN")
+    E0 = o.measurables()[0][0]
+    hs = []
+    for _ in range(6):
+        t0 = o.get_time()[0]
+        o.step(1)
+        err, _ = o.dp_stats()
+        assert err <= 1.0
+        hs.append(o.get_time()[0] - t0)
+    assert o.dp_stats()[1] >= 1
+    assert all(b <= 1.5 * a * (1 + 1e-12) for a, b in zip(hs, hs[1:]))
+    t = o.get_time()[0]
+    # Taylor–Green at early times: E(t) ~ E0 exp(-6 nu t)
+    assert abs(o.measurables()[0][0] / (E0 * np.exp(-6 * 0.01 * t)) - 1) < 5e-3
