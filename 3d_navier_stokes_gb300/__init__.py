@@ -46,6 +46,7 @@ EXPORTS = (
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
+    "ns3d_les_infer_host", "ns3d_les_profile_infer",
 )
 
 
@@ -202,6 +203,10 @@ def lib():
         L.ns3d_les_gradients_host.argtypes = [P, F, F, D, F]
         L.ns3d_les_forward_host.restype = I
         L.ns3d_les_forward_host.argtypes = [P, F, F]
+        L.ns3d_les_infer_host.restype = I
+        L.ns3d_les_infer_host.argtypes = [P, F, F]
+        L.ns3d_les_profile_infer.restype = I
+        L.ns3d_les_profile_infer.argtypes = [P, I, ctypes.POINTER(ctypes.c_float)]
         L.ns3d_les_attach.restype = I
         L.ns3d_les_attach.argtypes = [P, P]
         L.ns3d_les_counters.restype = I
@@ -563,7 +568,21 @@ class LES:
         return loss.value, g
 
     def forward(self, u: np.ndarray) -> np.ndarray:
+        """tau = network(u), FP32 training network."""
         u = np.ascontiguousarray(u, dtype=np.float32)
         out = np.empty((6,) + u.shape[1:], np.float32)
         self._ck(lib().ns3d_les_forward_host(self._h, _fp(u), _fp(out)))
+        return out
+
+    def profile_infer(self, reps: int = 10) -> float:
+        """Mean device milliseconds of one inference (device-resident input)."""
+        v = ctypes.c_float()
+        self._ck(lib().ns3d_les_profile_infer(self._h, reps, ctypes.byref(v)))
+        return v.value
+
+    def infer(self, u: np.ndarray) -> np.ndarray:
+        """tau = network(u) through the attached-run inference path (tensor cores for Nc in 16, 32, 64)."""
+        u = np.ascontiguousarray(u, dtype=np.float32)
+        out = np.empty((6,) + u.shape[1:], np.float32)
+        self._ck(lib().ns3d_les_infer_host(self._h, _fp(u), _fp(out)))
         return out

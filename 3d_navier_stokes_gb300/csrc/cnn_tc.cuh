@@ -1,0 +1,357 @@
+// cnn_tc.cuh — inference of the closure network on the 5th-generation tensor
+// cores. A 3^3 convolution
+//     out[p][co] = b[co] + sum_{dx,dy,dz} sum_ci in[p + (dx,dy,dz)][ci] W[co][ci][dx,dy,dz]
+// is computed as nine GEMMs over the (dx, dy) taps whose N dimension holds the
+// three dz taps side by side:
+//     G[q][dz*NO + co] = sum_{dx,dy} sum_ci in[q + (dx,dy,0)][ci] W[co][ci][dx,dy,dz]
+//     out[p][co] = G[p - 1z][0*NO + co] + G[p][1*NO + co] + G[p + 1z][2*NO + co]
+// M = 128 grid points per tile (R = 128/D whole z-lines at one x, D in
+// {16, 32, 64}), so the z neighbours of every row, periodic wrap included,
+// are rows of the same tile; N = 3 NO (96 for the 32-channel layers, 48 for
+// the 6-channel output padded to 16); K = the input channels, 16 per
+// tcgen05.mma kind::f16 (BF16 operands from shared memory, FP32 accumulator in
+// tensor memory), 9 x CIN/16 MMAs per tile issued by one thread.
+//
+// Shared-memory operand layout (SWIZZLE_NONE, K-major canonical form): a
+// "core matrix" is 8 rows x 16 bytes (8 rows of 8 BF16 channels), stored
+// contiguously; the KC core matrices of one 8-row group (the K direction)
+// are adjacent, so the descriptor's leading byte offset (K step) is 128 bytes
+// and its stride byte offset (next 8 rows) is KC * 128 bytes.
+//   A: [x plane 3][y row R+2][z group D/8][kchunk KC][8 points][16 B]  (x2, double buffered)
+//   B: [(dx,dy) 9][n group 3 NO/8][kchunk KC][8 (dz, co)][16 B]
+// Activations between layers are BF16 in the blocked layout
+// [x][y][z group][kchunk][8 points][8 channels], so every (x, y) line of the
+// halo block is one contiguous run identical to its place in A: one thread
+// stages a tile with 3 (R+2) cp.async.bulk copies completed on an mbarrier.
+// The copies for tile i+2 are issued as soon as the MMAs of tile i have
+// released its buffer, and the MMAs of tile i+1 before the epilogue of tile i
+// (tensor memory -> registers, the dz combination through a shared exchange
+// of the dz = -1 and +1 blocks, bias, GELU), which the other warps run while
+// the tensor cores work; two accumulators live in tensor memory. Layers
+// write GELU(z) in the blocked layout; k_to_blocked converts the FP32
+// velocity [3][D^3] (x in_scale) into the blocked form of layer 1, and the
+// output layer writes FP32 [6][D^3] (x out_scale). Every wait is bounded; on
+// a timeout the kernel records kStatusTimeout in *status, waits once more
+// (bounded) for its own copies and MMAs, frees its tensor memory and returns.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tma.cuh"
+
+namespace ns3d {
+namespace cnn {
+
+// ------------------------------------------------------------ tcgen05 PTX
+__device__ __forceinline__ void tmem_alloc(uint32_t* holder, uint32_t ncols) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(holder)),
+                 "r"(ncols)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_relinquish() {
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// D[tmem] (+)= A[smem] * B[smem]^T, BF16 x BF16 -> FP32
+__device__ __forceinline__ void mma_bf16(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+    asm volatile(
+        "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+        " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(idesc), "r"(acc)
+        : "memory");
+}
+// arrive on `bar` once every MMA issued so far by this thread has completed
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+// 32 lanes x 16 columns of 32 bits: thread i of the warp gets lane (quarter base + i)
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+}
+// wait for the tensor-memory loads; the registers pass through so that no use
+// of them is scheduled before the wait
+__device__ __forceinline__ void tmem_wait_ld(uint32_t (&r)[16]) {
+    asm volatile("tcgen05.wait::ld.sync.aligned;"
+                 : "+r"(r[0]), "+r"(r[1]), "+r"(r[2]), "+r"(r[3]), "+r"(r[4]), "+r"(r[5]), "+r"(r[6]), "+r"(r[7]),
+                   "+r"(r[8]), "+r"(r[9]), "+r"(r[10]), "+r"(r[11]), "+r"(r[12]), "+r"(r[13]), "+r"(r[14]),
+                   "+r"(r[15])
+                 :
+                 : "memory");
+}
+
+// shared-memory matrix descriptor: start address, leading (K) and stride
+// (M/N) byte offsets, descriptor version 1, no swizzle
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: FP32 accumulator, BF16 A and B, both K-major
+__host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ float gelu_tc(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t*>(&h);
+}
+
+constexpr int kTcTmemCols = 256;   // two accumulators of up to 96 columns, at 0 and 128
+
+__host__ __device__ constexpr bool tc_grid_ok(int D) { return D == 16 || D == 32 || D == 64; }
+__host__ __device__ constexpr uint32_t tc_a_bytes(int KC, int D) {
+    return 3u * (uint32_t)(128 / D + 2) * (uint32_t)D * (uint32_t)KC * 16u;
+}
+__host__ __device__ constexpr uint32_t tc_b_bytes(int KC, int NO) { return 9u * 3u * (uint32_t)NO * (uint32_t)KC * 16u; }
+__host__ __device__ constexpr uint32_t tc_x_bytes(int NO) { return 2u * (uint32_t)NO * 128u * 4u; }
+__host__ __device__ constexpr uint32_t tc_smem_bytes(int KC, int NO, int D) {
+    return tc_b_bytes(KC, NO) + 2u * tc_a_bytes(KC, D) + tc_x_bytes(NO) + 48u;
+}
+
+// blocked activation index (in 16-byte units) of point (x, y, z), chunk kc
+template <int LOGD, int KC>
+__device__ __forceinline__ long long blk_index(int x, int y, int z, int kc) {
+    constexpr int ZG = (1 << LOGD) / 8;
+    return (((((long long)x << LOGD) + y) * ZG + (z >> 3)) * KC + kc) * 8 + (z & 7);
+}
+
+// FP32 velocity [3][D^3] x in_scale -> blocked BF16 with 16 channels (KC = 2)
+template <int LOGD>
+__global__ void k_to_blocked(const float* __restrict__ u, float in_scale, uint4* __restrict__ dst) {
+    constexpr int D = 1 << LOGD;
+    constexpr long long D3 = (long long)D * D * D;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(p & (D - 1)), y = (int)((p >> LOGD) & (D - 1)), x = (int)(p >> (2 * LOGD));
+        uint4 v;
+        v.x = pack_bf16x2(u[p] * in_scale, u[D3 + p] * in_scale);
+        v.y = pack_bf16x2(u[2 * D3 + p] * in_scale, 0.0f);
+        v.z = 0u;
+        v.w = 0u;
+        dst[blk_index<LOGD, 2>(x, y, z, 0)] = v;
+        dst[blk_index<LOGD, 2>(x, y, z, 1)] = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// B operand of one layer from W[cout][cin][27] (BF16) in the shared-memory
+// order [(dx,dy) 9][n group][kchunk][8 n][8 channels], n = dz * NO + co;
+// zero padding to NO output and 8 KC input channels
+__global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cout, int cin, int KC, int NO,
+                          __nv_bfloat16* __restrict__ dst) {
+    const int NG = 3 * NO / 8;
+    const int n_all = 9 * NG * KC * 64;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_all; q += gridDim.x * blockDim.x) {
+        const int j = q % 8;
+        int r = q / 8;
+        const int n8 = r % 8;
+        r /= 8;
+        const int kc = r % KC;
+        r /= KC;
+        const int ng = r % NG;
+        const int t9 = r / NG;
+        const int n = ng * 8 + n8, dz = n / NO, co = n % NO, ci = kc * 8 + j;
+        const int t = t9 * 3 + dz;   // tap (dx+1)*9 + (dy+1)*3 + (dz+1)
+        dst[q] = (co < cout && ci < cin) ? w[((long long)co * cin + ci) * 27 + t] : __float2bfloat16(0.0f);
+    }
+}
+
+// One layer. KC: 16-byte channel chunks of the input (CIN padded to 8 KC);
+// NO: output channels per dz block (32, or 16 for the output layer);
+// D = 1 << LOGD; input BF16 blocked with KC chunks; OUT_MODE 0: GELU(out + b)
+// as BF16 blocked with 4 chunks, 1: (out + b) * out_scale as FP32
+// [cout][D^3]. 256 threads: thread 0 issues the copies and the MMAs, every
+// warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
+// channels [16 (w / 4), 16 (w / 4) + 16).
+constexpr int kTcThreads = 256;
+
+template <int KC, int NO, int LOGD, int OUT_MODE>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const float* __restrict__ bias,
+           void* __restrict__ out, int cout, float out_scale, int* __restrict__ status) {
+    static_assert(KC % 2 == 0 && (NO == 16 || NO == 32), "tile shape");
+    constexpr int D = 1 << LOGD, R = 128 / D, rows = R + 2, ZG = D / 8, NB = 3 * NO;
+    static_assert(R >= 1 && R <= D, "grid size");
+    constexpr uint32_t b_bytes = tc_b_bytes(KC, NO), a_bytes = tc_a_bytes(KC, D);
+    constexpr uint32_t line_bytes = (uint32_t)D * KC * 16;   // one (x, y) line of the blocked input
+    constexpr long long D3 = (long long)D * D * D;
+    constexpr int tiles_per_x = D / R, ntiles = D * tiles_per_x;
+    constexpr uint32_t idesc = idesc_bf16(128, NB);
+    extern __shared__ __align__(128) unsigned char smem[];
+    unsigned char* sB = smem;
+    unsigned char* sA = smem + b_bytes;                                        // two buffers
+    float* sX = reinterpret_cast<float*>(sA + 2 * a_bytes);                    // [2][NO][128]
+    uint64_t* done = reinterpret_cast<uint64_t*>(sA + 2 * a_bytes + tc_x_bytes(NO));   // MMAs of buffer b done
+    uint64_t* full = done + 2;                                                 // copies into buffer b landed
+    uint32_t* holder = reinterpret_cast<uint32_t*>(full + 2);
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+    for (uint32_t q = tid; q < b_bytes / 16; q += kTcThreads) reinterpret_cast<uint4*>(sB)[q] = wpk[q];
+    fence_proxy_async_smem();   // B (generic stores) -> visible to the tensor cores
+    if (tid == 0) {
+        for (int b = 0; b < 2; ++b) {
+            mbar_init(&done[b], 1);
+            mbar_init(&full[b], 1);
+        }
+        fence_barrier_init();
+        s_ok = 1;
+    }
+    if (warp == 0) {
+        tmem_alloc(holder, kTcTmemCols);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *holder;
+    const uint32_t sA_u = smem_u32(sA), sB_u = smem_u32(sB);
+    // thread 0 state
+    uint32_t ph_done[2] = {0u, 0u}, ph_full[2] = {0u, 0u};
+    bool mma_pending[2] = {false, false}, copy_pending[2] = {false, false};
+    bool ok = true;
+
+    // thread 0: the halo block of tile t into buffer b: 3 (R+2) line copies
+    auto load = [&](int t, int b) {
+        const int x = t / tiles_per_x, y0 = (t % tiles_per_x) * R;
+        mbar_arrive_expect_tx(&full[b], a_bytes);
+#pragma unroll 1
+        for (int l = 0; l < 3 * rows; ++l) {
+            const int xp = l / rows, yr = l % rows;
+            const int gx = (x + xp - 1) & (D - 1), gy = (y0 + yr - 1) & (D - 1);
+            bulk_g2s(sA + b * a_bytes + l * line_bytes, in + (((long long)gx << LOGD) + gy) * (D * KC), line_bytes,
+                     &full[b]);
+        }
+        copy_pending[b] = true;
+    };
+    // thread 0: wait for buffer b, then its 9 x KC/2 MMAs into accumulator b
+    auto issue = [&](int b) {
+        ok = ok && mbar_wait(&full[b], ph_full[b]);
+        ph_full[b] ^= 1u;
+        copy_pending[b] = false;
+        if (!ok) return;
+        const uint32_t a_base = sA_u + b * a_bytes, d = tmem + 128u * b;
+        uint32_t acc = 0;
+#pragma unroll 1
+        for (int t9 = 0; t9 < 9; ++t9) {
+            const int dx = t9 / 3, dy = t9 % 3;   // offsets + 1
+            const uint32_t a0 = a_base + ((dx * rows + dy) * ZG) * KC * 128;
+            const uint32_t b0 = sB_u + (uint32_t)(t9 * (NB / 8) * KC) * 128;
+#pragma unroll
+            for (int ks = 0; ks < KC / 2; ++ks) {
+                mma_bf16(d, smem_desc(a0 + ks * 256, 128, KC * 128), smem_desc(b0 + ks * 256, 128, KC * 128), idesc,
+                         acc);
+                acc = 1;
+            }
+        }
+        mma_commit(&done[b]);
+        mma_pending[b] = true;
+    };
+
+    // tile i lives in buffer and accumulator i % 2; its copies are issued one
+    // iteration ahead, as soon as the MMAs of tile i - 2 have released the buffer
+    int tile = blockIdx.x;
+    if (tid == 0) {
+        if (tile < ntiles) load(tile, 0);
+        if (tile + (int)gridDim.x < ntiles) load(tile + gridDim.x, 1);
+        if (tile < ntiles) issue(0);
+    }
+    for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
+        const int b = it & 1, nb = b ^ 1;
+        const int next = tile + gridDim.x, next2 = next + gridDim.x;
+        if (tid == 0) {
+            if (ok) ok = mbar_wait(&done[b], ph_done[b]);
+            ph_done[b] ^= 1u;
+            mma_pending[b] = false;
+            // buffer b is free again; accumulator nb was read by the previous epilogue
+            if (ok && next2 < ntiles) load(next2, b);
+            if (ok && next < ntiles) issue(nb);
+            if (!ok) {
+                atomicExch(status, kStatusTimeout);
+                s_ok = 0;
+            }
+        }
+        __syncwarp();
+        __syncthreads();
+        if (!s_ok) break;
+        tc_fence_after();
+        // ---- epilogue of this tile
+        const int x = tile / tiles_per_x, y0 = (tile % tiles_per_x) * R;
+        const int quarter = warp & 3, half = warp >> 2;
+        const int m = quarter * 32 + lane;
+        const bool active = (NO == 32) || half == 0;
+        const uint32_t tl = tmem + 128u * b + ((uint32_t)(quarter * 32) << 16) + 16u * half;
+        uint32_t gm[16], g0[16], gp[16];
+        if (active) {
+            tmem_ld16(tl, gm);
+            tmem_ld16(tl + NO, g0);
+            tmem_ld16(tl + 2 * NO, gp);
+            tmem_wait_ld(gm);
+            tmem_wait_ld(g0);
+            tmem_wait_ld(gp);
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                sX[(16 * half + j) * 128 + m] = __uint_as_float(gm[j]);
+                sX[(NO + 16 * half + j) * 128 + m] = __uint_as_float(gp[j]);
+            }
+        }
+        tc_fence_before();
+        __syncthreads();
+        if (active) {
+            const int line = m & ~(D - 1), zz = m & (D - 1), yy = y0 + (m >> LOGD);
+            const int left = line | ((zz - 1) & (D - 1)), right = line | ((zz + 1) & (D - 1));
+            float v[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+                const int co = 16 * half + j;
+                v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] +
+                       bias[co < cout ? co : 0];
+            }
+            if constexpr (OUT_MODE == 0) {
+                uint4* dst = reinterpret_cast<uint4*>(out);
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] =
+                        make_uint4(pack_bf16x2(gelu_tc(v[q * 8 + 0]), gelu_tc(v[q * 8 + 1])),
+                                   pack_bf16x2(gelu_tc(v[q * 8 + 2]), gelu_tc(v[q * 8 + 3])),
+                                   pack_bf16x2(gelu_tc(v[q * 8 + 4]), gelu_tc(v[q * 8 + 5])),
+                                   pack_bf16x2(gelu_tc(v[q * 8 + 6]), gelu_tc(v[q * 8 + 7])));
+            } else {
+                float* dst = reinterpret_cast<float*>(out);
+                const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
+#pragma unroll
+                for (int j = 0; j < 16; ++j)
+                    if (j < cout) dst[j * D3 + p] = v[j] * out_scale;
+            }
+        }
+        // the exchange buffer and this accumulator are free before their next use
+        tc_fence_before();
+        __syncthreads();
+        tc_fence_after();
+    }
+    // after a failed wait: one more bounded wait for the copies and MMAs in flight
+    if (tid == 0) {
+#pragma unroll
+        for (int b = 0; b < 2; ++b) {
+            if (copy_pending[b]) mbar_wait(&full[b], ph_full[b]);
+            if (mma_pending[b]) mbar_wait(&done[b], ph_done[b]);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, kTcTmemCols);
+}
+
+}  // namespace cnn
+}  // namespace ns3d

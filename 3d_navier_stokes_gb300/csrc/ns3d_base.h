@@ -15,6 +15,8 @@ namespace ns3d {
 struct LesHook {
     virtual ~LesHook() {}
     virtual void forward(const float* u, float* tau, int N, cudaStream_t s) = 0;
+    // device word that the closure's kernels set to a non-zero status on failure
+    virtual int* status_word() = 0;
 };
 
 class Base {

@@ -228,7 +228,7 @@ class Impl final : public Base {
                 W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr, nullptr, nullptr, RkStage{});
         }
         k_sgs_div<T, N><<<kSgsParts, 256, 0, s_>>>(TAU_, U_, F_, sgs_part_);
-        k_sgs_flag<><<<1, 32, 0, s_>>>(sgs_part_, kSgsParts, sd_);
+        k_sgs_flag<><<<1, 32, 0, s_>>>(sgs_part_, kSgsParts, sd_, les_->status_word());
     }
     static constexpr int kSgsParts = 512;
 

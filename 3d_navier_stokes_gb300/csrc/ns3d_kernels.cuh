@@ -1320,11 +1320,14 @@ __global__ void k_sgs_div(const cx<T>* __restrict__ TAU, const cx<T>* __restrict
 // removes energy on balance (T <= 0) and is finite; otherwise this step is
 // the plain coarse solve
 template <int Unused = 0>
-__global__ void k_sgs_flag(const double* __restrict__ part, int nparts, StepDev* __restrict__ sd) {
+__global__ void k_sgs_flag(const double* __restrict__ part, int nparts, StepDev* __restrict__ sd,
+                           const int* __restrict__ les_status) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double s = 0.0;
     for (int i = 0; i < nparts; ++i) s += part[i];
-    const int ok = isfinite(s) && s <= 0.0;
+    // a closure kernel that gave up on a bounded wait fails the step
+    if (les_status && *les_status != 0) sd->status = kStatusTimeout;
+    const int ok = isfinite(s) && s <= 0.0 && !(les_status && *les_status != 0);
     sd->sgs_on = ok;
     if (ok) sd->sgs_steps += 1;
     else sd->sgs_fallbacks += 1;

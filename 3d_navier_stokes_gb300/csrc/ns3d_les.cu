@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "cnn.cuh"
+#include "cnn_tc.cuh"
 #include "ns3d_ctx.h"
 
 namespace ns3d {
@@ -81,6 +82,10 @@ constexpr int C = 32;   // hidden channels
 constexpr int oW1 = 0, ob1 = oW1 + C * 3 * 27, oW2 = ob1 + C, ob2 = oW2 + C * C * 27, oW3 = ob2 + C,
               ob3 = oW3 + C * C * 27, oW4 = ob3 + C, ob4 = oW4 + 6 * C * 27, NPARAM = ob4 + 6;
 constexpr int NPART = 256;
+// packed tensor-core B operands of the four layers (BF16 elements):
+// (KC, NO) = (2, 32), (4, 32), (4, 32), (4, 16); 9 x 3 NO x 8 KC each
+constexpr int kTcW1 = 9 * 96 * 2 * 8, kTcW2 = 9 * 96 * 4 * 8, kTcW4 = 9 * 48 * 4 * 8;
+constexpr int oT1 = 0, oT2 = oT1 + kTcW1, oT3 = oT2 + kTcW2, oT4 = oT3 + kTcW2, kTcWTotal = oT4 + kTcW4;
 
 unsigned long long sm64(unsigned long long& s) {
     unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
@@ -100,6 +105,11 @@ struct ns3d_les : public ns3d::LesHook {
           *gz2 = nullptr, *gz1 = nullptr, *io_u = nullptr, *io_t = nullptr;
     double* part = nullptr;
     double* part_host = nullptr;
+    // tensor-core inference (Nc in {16, 32, 64})
+    __nv_bfloat16* wtc = nullptr;                        // packed B operands
+    __nv_bfloat16 *act0 = nullptr, *act1 = nullptr, *act2 = nullptr, *act3 = nullptr;   // blocked BF16 activations
+    int* dstat = nullptr;                                // device status word
+    int tc_grid[3] = {0, 0, 0};                          // CTAs of the three kernel shapes
     double s_in = 1.0, s_out = 1.0;
     bool scales_set = false;
     long long adam_t = 0;
@@ -138,20 +148,89 @@ struct ns3d_les : public ns3d::LesHook {
         return l / (double)(6 * D3);
     }
 
+    bool tc() const { return ns3d::cnn::tc_grid_ok(Nc) && wtc != nullptr; }
+
+    // B operands of the tensor-core layers from the current BF16 weights
+    void pack_tc(cudaStream_t s) {
+        if (!tc()) return;
+        using ns3d::cnn::k_pack_tc;
+        k_pack_tc<<<64, 256, 0, s>>>(wb + oW1, C, 3, 2, 32, wtc + oT1);
+        k_pack_tc<<<64, 256, 0, s>>>(wb + oW2, C, C, 4, 32, wtc + oT2);
+        k_pack_tc<<<64, 256, 0, s>>>(wb + oW3, C, C, 4, 32, wtc + oT3);
+        k_pack_tc<<<64, 256, 0, s>>>(wb + oW4, 6, C, 4, 16, wtc + oT4);
+    }
+
+    // tensor-core inference: four implicit-GEMM convolutions on blocked BF16 activations
+    template <int LOGD>
+    void infer_tc_d(const float* u, float* tau, float in_scale, float out_scale, cudaStream_t s) {
+        using namespace ns3d::cnn;
+        constexpr int D = 1 << LOGD;
+        const uint4* W = reinterpret_cast<const uint4*>(wtc);
+        uint4* a0 = reinterpret_cast<uint4*>(act0);
+        uint4* a1 = reinterpret_cast<uint4*>(act1);
+        uint4* a2 = reinterpret_cast<uint4*>(act2);
+        uint4* a3 = reinterpret_cast<uint4*>(act3);
+        k_to_blocked<LOGD><<<(unsigned)((D3 + 255) / 256), 256, 0, s>>>(u, in_scale, a0);
+        k_conv3_tc<2, 32, LOGD, 0><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+            a0, W + oT1 / 8, w + ob1, a1, C, 1.f, dstat);
+        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            a1, W + oT2 / 8, w + ob2, a2, C, 1.f, dstat);
+        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            a2, W + oT3 / 8, w + ob3, a3, C, 1.f, dstat);
+        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kTcThreads, tc_smem_bytes(4, 16, D), s>>>(
+            a3, W + oT4 / 8, w + ob4, tau, 6, out_scale, dstat);
+    }
+    void infer_tc(const float* u, float* tau, float in_scale, float out_scale, cudaStream_t s) {
+        if (Nc == 16) infer_tc_d<4>(u, tau, in_scale, out_scale, s);
+        else if (Nc == 32) infer_tc_d<5>(u, tau, in_scale, out_scale, s);
+        else infer_tc_d<6>(u, tau, in_scale, out_scale, s);
+    }
+
     void forward(const float* u, float* tau, int N, cudaStream_t s) override {
         (void)N;
-        fwd(u, tau, (float)(1.0 / s_in), (float)s_out, s);
+        if (tc()) infer_tc(u, tau, (float)(1.0 / s_in), (float)s_out, s);
+        else fwd(u, tau, (float)(1.0 / s_in), (float)s_out, s);
     }
+    int* status_word() override { return dstat; }
 
     ~ns3d_les() override {
         for (void* q : {(void*)data_u, (void*)data_t, (void*)w, (void*)g, (void*)m, (void*)v, (void*)wb, (void*)z1,
                         (void*)z2, (void*)z3, (void*)y, (void*)gy, (void*)gz3, (void*)gz2, (void*)gz1, (void*)io_u,
-                        (void*)io_t, (void*)part})
+                        (void*)io_t, (void*)part, (void*)wtc, (void*)act0, (void*)act1, (void*)act2, (void*)act3,
+                        (void*)dstat})
             if (q) cudaFree(q);
         if (part_host) cudaFreeHost(part_host);
         if (stream) cudaStreamDestroy(stream);
     }
 };
+
+// shared-memory opt-in and persistent grid sizes of the tensor-core kernels
+template <int LOGD>
+static ns3d_status les_tc_setup_d(ns3d_les* l, int nsm) {
+    using namespace ns3d::cnn;
+    constexpr int D = 1 << LOGD, ntiles = D * D * D / 128;
+    const void* fns[3] = {(const void*)k_conv3_tc<2, 32, LOGD, 0>, (const void*)k_conv3_tc<4, 32, LOGD, 0>,
+                          (const void*)k_conv3_tc<4, 16, LOGD, 1>};
+    const uint32_t sm[3] = {tc_smem_bytes(2, 32, D), tc_smem_bytes(4, 32, D), tc_smem_bytes(4, 16, D)};
+    for (int k = 0; k < 3; ++k) {
+        if (cudaFuncSetAttribute(fns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm[k]) != cudaSuccess)
+            return NS3D_ERR_CUDA;
+        int per = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fns[k], kTcThreads, sm[k]) != cudaSuccess || per < 1)
+            return NS3D_ERR_CUDA;
+        l->tc_grid[k] = per * nsm < ntiles ? per * nsm : ntiles;
+    }
+    return NS3D_OK;
+}
+
+static ns3d_status les_tc_setup(ns3d_les* l) {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return NS3D_ERR_CUDA;
+    if (l->Nc == 16) return les_tc_setup_d<4>(l, nsm);
+    if (l->Nc == 32) return les_tc_setup_d<5>(l, nsm);
+    return les_tc_setup_d<6>(l, nsm);
+}
 
 static ns3d_status les_fail(ns3d_les* l, ns3d_status s, const char* msg) {
     if (l) snprintf(l->err, sizeof(l->err), "%s", msg);
@@ -210,6 +289,22 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
     cudaMemset(l->m, 0, f * NPARAM);
     cudaMemset(l->v, 0, f * NPARAM);
     ns3d::cnn::k_to_bf16<<<(NPARAM + 255) / 256, 256, 0, l->stream>>>(l->w, l->wb, NPARAM);
+    if (cudaMalloc(&l->dstat, sizeof(int)) != cudaSuccess || cudaMemset(l->dstat, 0, sizeof(int)) != cudaSuccess) {
+        delete l;
+        return NS3D_ERR_NOMEM;
+    }
+    if (ns3d::cnn::tc_grid_ok(Nc)) {
+        const size_t a = sizeof(__nv_bfloat16) * C * (size_t)l->D3;
+        if (cudaMalloc(&l->wtc, sizeof(__nv_bfloat16) * kTcWTotal) != cudaSuccess || cudaMalloc(&l->act0, a / 2) != cudaSuccess ||
+            cudaMalloc(&l->act1, a) != cudaSuccess ||
+            cudaMalloc(&l->act2, a) != cudaSuccess || cudaMalloc(&l->act3, a) != cudaSuccess ||
+            les_tc_setup(l) != NS3D_OK) {
+            delete l;
+            cudaGetLastError();
+            return NS3D_ERR_NOMEM;
+        }
+        l->pack_tc(l->stream);
+    }
     if (cudaStreamSynchronize(l->stream) != cudaSuccess) {
         delete l;
         return NS3D_ERR_CUDA;
@@ -319,6 +414,7 @@ ns3d_status ns3d_les_train(ns3d_les* l, int iterations, double lr, double* mean_
             nacc++;
         }
     }
+    l->pack_tc(l->stream);
     LES_CK(cudaStreamSynchronize(l->stream));
     if (mean_loss) *mean_loss = nacc ? acc / nacc : 0.0;
     return NS3D_OK;
@@ -348,6 +444,7 @@ ns3d_status ns3d_les_weights_host(ns3d_les* l, float* w, int set) {
     if (set) {
         LES_CK(cudaMemcpy(l->w, w, sizeof(float) * NPARAM, cudaMemcpyHostToDevice));
         ns3d::cnn::k_to_bf16<<<(NPARAM + 255) / 256, 256, 0, l->stream>>>(l->w, l->wb, NPARAM);
+        l->pack_tc(l->stream);
         LES_CK(cudaStreamSynchronize(l->stream));
     } else {
         LES_CK(cudaMemcpy(w, l->w, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost));
@@ -368,9 +465,40 @@ ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* ta
 ns3d_status ns3d_les_forward_host(ns3d_les* l, const float* u, float* tau) {
     if (!l || !u || !tau) return NS3D_ERR_INVALID;
     LES_CK(cudaMemcpy(l->io_u, u, sizeof(float) * 3 * l->D3, cudaMemcpyHostToDevice));
-    l->forward(l->io_u, l->io_t, l->Nc, l->stream);
+    l->fwd(l->io_u, l->io_t, (float)(1.0 / l->s_in), (float)l->s_out, l->stream);
     LES_CK(cudaStreamSynchronize(l->stream));
     LES_CK(cudaMemcpy(tau, l->io_t, sizeof(float) * 6 * l->D3, cudaMemcpyDeviceToHost));
+    return NS3D_OK;
+}
+
+ns3d_status ns3d_les_infer_host(ns3d_les* l, const float* u, float* tau) {
+    if (!l || !u || !tau) return NS3D_ERR_INVALID;
+    LES_CK(cudaMemcpy(l->io_u, u, sizeof(float) * 3 * l->D3, cudaMemcpyHostToDevice));
+    l->forward(l->io_u, l->io_t, l->Nc, l->stream);
+    LES_CK(cudaStreamSynchronize(l->stream));
+    int st = 0;
+    LES_CK(cudaMemcpy(&st, l->dstat, sizeof(int), cudaMemcpyDeviceToHost));
+    if (st != 0) return les_fail(l, NS3D_ERR_TIMEOUT, "a bounded wait in the tensor-core convolution gave up");
+    LES_CK(cudaMemcpy(tau, l->io_t, sizeof(float) * 6 * l->D3, cudaMemcpyDeviceToHost));
+    return NS3D_OK;
+}
+
+ns3d_status ns3d_les_profile_infer(ns3d_les* l, int reps, float* ms) {
+    if (!l || reps <= 0 || !ms) return NS3D_ERR_INVALID;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    LES_CK(cudaEventCreate(&e0));
+    LES_CK(cudaEventCreate(&e1));
+    l->forward(l->io_u, l->io_t, l->Nc, l->stream);   // warm-up
+    cudaEventRecord(e0, l->stream);
+    for (int r = 0; r < reps; ++r) l->forward(l->io_u, l->io_t, l->Nc, l->stream);
+    cudaEventRecord(e1, l->stream);
+    cudaError_t e = cudaEventSynchronize(e1);
+    float t = 0.f;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (e != cudaSuccess) return les_fail(l, NS3D_ERR_CUDA, cudaGetErrorString(e));
+    *ms = t / (float)reps;
     return NS3D_OK;
 }
 

@@ -46,9 +46,10 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256"])
-    ap.add_argument("--snapshots", type=int, default=200)
+    ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
-    ap.add_argument("--les-steps", type=int, default=1000)
+    ap.add_argument("--les-steps", type=int, default=2000)
+    ap.add_argument("--decay-steps", type=int, default=1000)
     return ap.parse_args()
 
 
@@ -390,6 +391,7 @@ def run_les(args, local):
     ms = {}
     dns.RK4Step(args.les_steps)
     ms["dns"] = dns.last_step_ms() / args.les_steps
+    ms["closure_inference"] = les.profile_infer(20)
     for n, c in runs.items():
         c.RK4Step(args.les_steps)
         ms[n] = c.last_step_ms() / args.les_steps
@@ -407,7 +409,9 @@ def run_les(args, local):
             "plain_coarse_error": err["plain"], "n_gpus": 1, "steps": args.les_steps, "dtype": "f32 (bf16 weights)",
             "data": "synthetic", "config": {"workload": "learned closure C5", "dns_N": Nf, "les_N": Nc, "nu": nu,
                                             "dt": dt, "snapshots": args.snapshots, "train_iters": args.train_iters},
-            "ms_per_step": {"dns_256": ms["dns"], "les_64_closure": ms["closure"], "plain_64": ms["plain"]},
+            "ms_per_step": {"dns_256": ms["dns"], "les_64_closure": ms["closure"], "plain_64": ms["plain"],
+                            "closure_inference": ms["closure_inference"]},
+            "inference_tflops": 126144.0 * Nc ** 3 / (ms["closure_inference"] * 1e-3) / 1e12,
             "speedup_vs_dns": ms["dns"] / ms["closure"], "closure_steps": on, "fallback_steps": off,
             "loss": {"before": loss0, "after": loss1, "train_tail": loss_tr},
             "seconds": {"data": t_data, "train": t_train}}
@@ -417,7 +421,7 @@ def run_les(args, local):
 
 def run_decay(args, local):
     """Config C2: decaying turbulence at 256^3 (SPECTRUM IC k0 = 4, nu = 2e-3, CFL 0.5, IF-RK4,
-    --les-steps steps) in FP64 and in FP32; reports the FP32 relative errors of the energy, the
+    --decay-steps steps) in FP64 and in FP32; reports the FP32 relative errors of the energy, the
     dissipation and E(k) against FP64, and both step rates."""
     import importlib
     import numpy as np
@@ -425,7 +429,7 @@ def run_decay(args, local):
 
     pkg = importlib.import_module("3d_navier_stokes_gb300")
     torch.cuda.set_device(local)
-    N, steps = 256, args.les_steps
+    N, steps = 256, args.decay_steps
     res = {}
     for prec in ("fp64", "fp32"):
         s = pkg.Solver(N, nu=2e-3, dt=1e-3, cfl=0.5, precision=prec, device=local)

@@ -216,8 +216,14 @@ ns3d_status ns3d_les_dataset_loss(ns3d_les* l, double* mean_loss);
 ns3d_status ns3d_les_weights_host(ns3d_les* l, float* w, int set);
 /* loss and weight gradients for one sample (u [3][Nc^3], tau [6][Nc^3] host floats) */
 ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* tau, double* loss, float* grads);
-/* tau = network(u) in physical units */
+/* tau = network(u) in physical units, the FP32 training network (FP32 activations) */
 ns3d_status ns3d_les_forward_host(ns3d_les* l, const float* u, float* tau);
+/* tau = network(u) through the inference path an attached coarse run uses: for
+ * Nc in {16, 32, 64} tensor-core convolutions (BF16 activations and weights,
+ * FP32 accumulation), otherwise the FP32 network */
+ns3d_status ns3d_les_infer_host(ns3d_les* l, const float* u, float* tau);
+/* mean device time (CUDA events) of one inference on device-resident input over reps calls */
+ns3d_status ns3d_les_profile_infer(ns3d_les* l, int reps, float* ms);
 /* attach the closure to a coarse FP32 context of grid Nc (NULL detaches) */
 ns3d_status ns3d_les_attach(ns3d_ctx* coarse, ns3d_les* l);
 /* steps taken with the closure and steps that fell back to the plain solve */

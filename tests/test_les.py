@@ -58,6 +58,25 @@ def test_cnn_gradients_and_forward_vs_cpu(ns3d):
     les.close()
 
 
+@pytest.mark.parametrize("D", [16, 32, 64])
+def test_tensor_core_inference_vs_fp32_network(ns3d, D):
+    """The attached-run inference path (tcgen05 implicit-GEMM convolutions,
+    BF16 activations and weights, FP32 accumulation) against the FP32 network
+    with the same BF16 weights: differences are BF16 roundings of the
+    activations only."""
+    les = ns3d.LES(D, capacity=0, seed=11)
+    les.set_scales(1.1, 0.9)
+    rng = np.random.default_rng(D)
+    u = rng.standard_normal((3, D, D, D)).astype(np.float32)
+    ref = les.forward(u)
+    got = les.infer(u)
+    assert np.isfinite(got).all()
+    rel_l2 = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel_l2 < 1e-2, rel_l2
+    assert np.abs(got - ref).max() < 5e-2 * np.abs(ref).max()
+    les.close()
+
+
 def test_box_filter(ns3d):
     Nf, Nc = 32, 8
     fine = ns3d.Solver(Nf, nu=0.01, precision="fp32")
