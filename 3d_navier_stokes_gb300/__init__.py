@@ -46,7 +46,7 @@ EXPORTS = (
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
-    "ns3d_les_infer_host", "ns3d_les_profile_infer",
+    "ns3d_les_infer_host", "ns3d_les_profile_infer", "ns3d_io_bytes",
 )
 
 
@@ -141,6 +141,8 @@ def lib():
         L.ns3d_set_dp_tolerances.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.ns3d_dp_stats.restype = I
         L.ns3d_dp_stats.argtypes = [P, D, ctypes.POINTER(ctypes.c_long)]
+        L.ns3d_io_bytes.restype = I
+        L.ns3d_io_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
         L.ns3d_stream.restype = P
         L.ns3d_stream.argtypes = [P]
         L.ns3d_kernels_per_step.restype = I
@@ -369,6 +371,12 @@ class Solver:
         v = ctypes.c_double()
         self._ck(lib().ns3d_max_speed_sum(self._h, ctypes.byref(v)))
         return v.value
+
+    def io_bytes(self):
+        """(host->device, device->host) bytes moved over the host link by the last upload / download."""
+        a, b = ctypes.c_longlong(), ctypes.c_longlong()
+        self._ck(lib().ns3d_io_bytes(self._h, ctypes.byref(a), ctypes.byref(b)))
+        return a.value, b.value
 
     def set_dp_tolerances(self, atol: float, rtol: float):
         """DP5CN error tolerances (DP_ABS_TOL, DP_REL_TOL; default 1e-7 each)."""

@@ -261,6 +261,11 @@ ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* c, double atol, double rtol) {
     return pass(c, c->impl->set_dp_tolerances(atol, rtol));
 }
 
+ns3d_status ns3d_io_bytes(ns3d_ctx* c, long long* h2d, long long* d2h) {
+    if (!c) return NS3D_ERR_INVALID;
+    return pass(c, c->impl->io_bytes(h2d, d2h));
+}
+
 ns3d_status ns3d_dp_stats(ns3d_ctx* c, double* last_err, long* rejects) {
     if (!c) return NS3D_ERR_INVALID;
     return pass(c, c->impl->dp_stats(last_err, rejects));

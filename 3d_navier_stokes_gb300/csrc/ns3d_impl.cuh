@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "ns3d_base.h"
@@ -69,7 +70,7 @@ class Impl final : public Base {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
                         (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
-                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_})
+                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_ranges_})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -474,24 +475,135 @@ class Impl final : public Base {
         if (!stage_) NS3D_CK(cudaMalloc(&stage_, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1)));
         return NS3D_OK;
     }
+    static constexpr long long kRefBytes = 48LL * N * N * (N / 2 + 1);   // reference Fourier array
+    // device address of a page-locked host array (16-byte aligned), else nullptr
+    static const void* host_dev_ptr(const void* h) {
+        cudaPointerAttributes a, z;
+        const unsigned char* last = static_cast<const unsigned char*>(h) + kRefBytes - 1;
+        if (cudaPointerGetAttributes(&a, h) != cudaSuccess || cudaPointerGetAttributes(&z, last) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        // the whole array must lie in one page-locked allocation mapped for the device
+        if (a.type != cudaMemoryTypeHost || z.type != cudaMemoryTypeHost || !a.devicePointer || !z.devicePointer ||
+            static_cast<const unsigned char*>(z.devicePointer) - static_cast<const unsigned char*>(a.devicePointer) !=
+                kRefBytes - 1 ||
+            (reinterpret_cast<uintptr_t>(h) & 15))
+            return nullptr;
+        return a.devicePointer;
+    }
     ns3d_status upload(const double* host, cx<T>* dst) {
+        if (const void* d = host_dev_ptr(host)) {
+            // the packing kernel reads the dealiased modes straight from the host array
+            k_pack<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(static_cast<const double2*>(d), dst);
+            NS3D_CK(cudaGetLastError());
+            io_h2d_ = sphere_bytes();
+            return NS3D_OK;
+        }
         ns3d_status st = ensure_stage();
         if (st != NS3D_OK) return st;
-        NS3D_CK(cudaMemcpyAsync(stage_, host, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1),
-                                cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaMemcpyAsync(stage_, host, kRefBytes, cudaMemcpyHostToDevice, s_));
         k_pack<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(stage_, dst);
         NS3D_CK(cudaGetLastError());
+        io_h2d_ = kRefBytes;
         return NS3D_OK;
     }
     ns3d_status download(const cx<T>* src, double* host) {
+        if (const void* d = host_dev_ptr(host)) {
+            ns3d_status st = line_plan((int)(reinterpret_cast<uintptr_t>(host) & 127));
+            if (st != NS3D_OK) return st;
+            k_unpack_lines<T, N><<<(unsigned)((plan_nr_ * 32LL + 255) / 256), 256, 0, s_>>>(
+                src, static_cast<double2*>(const_cast<void*>(d)), plan_ranges_, plan_nr_);
+            NS3D_CK(cudaGetLastError());
+            zero_host_lines(reinterpret_cast<unsigned char*>(host));   // host threads, during the GPU work
+            NS3D_CK(cudaStreamSynchronize(s_));
+            NS3D_CK(cudaGetLastError());
+            io_d2h_ = plan_gpu_bytes_;
+            return NS3D_OK;
+        }
         ns3d_status st = ensure_stage();
         if (st != NS3D_OK) return st;
         k_unpack<T, N><<<grid_for((long long)N * N * (N / 2 + 1)), 256, 0, s_>>>(src, stage_);
-        NS3D_CK(cudaMemcpyAsync(host, stage_, sizeof(double2) * 3 * (size_t)N * N * (N / 2 + 1),
-                                cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaMemcpyAsync(host, stage_, kRefBytes, cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         NS3D_CK(cudaGetLastError());
+        io_d2h_ = kRefBytes;
         return NS3D_OK;
+    }
+    // bytes of the dealiased modes in the reference layout
+    static long long sphere_bytes() {
+        long long n = 0;
+        for (int i = 0; i < N; ++i)
+            for (int j = 0; j < N; ++j) {
+                const int kx = i <= N / 2 ? i : i - N, ky = j <= N / 2 ? j : j - N;
+                const long long rem = (long long)G::KC2 - kx * kx - ky * ky;
+                if (rem >= 0) n += isqrt(rem) + 1;
+            }
+        return 48 * n;
+    }
+    static long long isqrt(long long v) {
+        long long r = (long long)std::sqrt((double)v);
+        while (r * r > v) --r;
+        while ((r + 1) * (r + 1) <= v) ++r;
+        return r;
+    }
+    // Split of the reference Fourier array between the GPU and host threads for
+    // a host array whose address is `align` mod 128: for every (kx, ky) row
+    // with dealiased modes the GPU writes the 128-byte lines that hold them
+    // (zeros included where a line extends past them); host threads zero all
+    // other bytes. The two sets of lines are disjoint.
+    ns3d_status line_plan(int align) {
+        if (plan_align_ == align) return NS3D_OK;
+        constexpr int NF = N / 2 + 1;
+        constexpr long long RB = 48LL * NF;
+        std::vector<longlong2> ranges;
+        plan_cpu_.clear();
+        long long cursor = 0, gpu = 0;
+        for (long long r = 0; r < (long long)N * N; ++r) {
+            const int i = (int)(r / N), j = (int)(r % N);
+            const int kx = i <= N / 2 ? i : i - N, ky = j <= N / 2 ? j : j - N;
+            const long long rem = (long long)G::KC2 - kx * kx - ky * ky;
+            if (rem < 0) continue;
+            const long long bs = r * RB, be = bs + 48 * (isqrt(rem) + 1);
+            long long ls = (align + bs) / 128 * 128 - align, le = (align + be + 127) / 128 * 128 - align;
+            if (ls < cursor) ls = cursor;
+            if (le > kRefBytes) le = kRefBytes;
+            if (ls >= le) continue;
+            if (cursor < ls) plan_cpu_.push_back({cursor, ls - cursor});
+            ranges.push_back(make_longlong2(ls / 16, le / 16));
+            gpu += le - ls;
+            cursor = le;
+        }
+        if (cursor < kRefBytes) plan_cpu_.push_back({cursor, kRefBytes - cursor});
+        if (plan_ranges_) cudaFree(plan_ranges_);
+        plan_ranges_ = nullptr;
+        NS3D_CK(cudaMalloc(&plan_ranges_, sizeof(longlong2) * ranges.size()));
+        NS3D_CK(cudaMemcpy(plan_ranges_, ranges.data(), sizeof(longlong2) * ranges.size(), cudaMemcpyHostToDevice));
+        plan_nr_ = (int)ranges.size();
+        plan_gpu_bytes_ = gpu;
+        plan_align_ = align;
+        return NS3D_OK;
+    }
+    // zero the host-owned bytes with up to 16 threads, split evenly by bytes
+    void zero_host_lines(unsigned char* host) const {
+        long long total = 0;
+        for (const auto& seg : plan_cpu_) total += seg.second;
+        unsigned nt = std::thread::hardware_concurrency();
+        nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
+        if (total < (1LL << 22)) nt = 1;
+        auto work = [&](long long lo, long long hi) {
+            long long pos = 0;
+            for (const auto& seg : plan_cpu_) {
+                const long long a = pos > lo ? pos : lo, b = pos + seg.second < hi ? pos + seg.second : hi;
+                if (a < b) memset(host + seg.first + (a - pos), 0, (size_t)(b - a));
+                pos += seg.second;
+                if (pos >= hi) break;
+            }
+        };
+        std::vector<std::thread> th;
+        for (unsigned t = 1; t < nt; ++t) th.emplace_back(work, total * t / nt, total * (t + 1) / nt);
+        work(0, total / nt);
+        for (auto& x : th) x.join();
     }
     static unsigned grid_for(long long n) {
         long long g = (n + 255) / 256;
@@ -678,6 +790,11 @@ class Impl final : public Base {
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
+    ns3d_status io_bytes(long long* h2d, long long* d2h) override {
+        if (h2d) *h2d = io_h2d_;
+        if (d2h) *d2h = io_d2h_;
+        return NS3D_OK;
+    }
     ns3d_status set_dp_tolerances(double atol, double rtol) override {
         NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev) * M_, cudaMemcpyDeviceToHost, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
@@ -798,6 +915,12 @@ class Impl final : public Base {
     double* sgs_part_ = nullptr;
     cx<T>* K_ = nullptr;           // RK5 family: stored stages [member][6][3]
     double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]
+    // host-array transfers
+    long long io_h2d_ = 0, io_d2h_ = 0;
+    int plan_align_ = -1, plan_nr_ = 0;
+    long long plan_gpu_bytes_ = 0;
+    longlong2* plan_ranges_ = nullptr;
+    std::vector<std::pair<long long, long long>> plan_cpu_;
     int M_ = 1;                    // members
     int m_ = 0;                    // selected member
     std::vector<ns3d_params> mp_;  // per-member parameters

@@ -1145,6 +1145,35 @@ __global__ void k_unpack(const cx<T>* __restrict__ U, double2* __restrict__ ref)
     }
 }
 
+// device -> host array (reference layout) over a list of 16-byte unit ranges:
+// every unit of the listed ranges gets its mode's value (zero outside the
+// sphere); one warp per range. The ranges cover whole 128-byte lines around
+// the dealiased modes; the host zeroes every other line.
+template <typename T, int N>
+__global__ void k_unpack_lines(const cx<T>* __restrict__ U, double2* __restrict__ ref,
+                               const longlong2* __restrict__ ranges, int nranges) {
+    using G = Geo<N>;
+    constexpr int NF = N / 2 + 1;
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nranges) return;
+    const longlong2 rg = ranges[w];
+    for (long long u = rg.x + lane; u < rg.y; u += 32) {
+        const long long e = u / 3;
+        const int c = (int)(u % 3);
+        const long long ij = e / NF;
+        const int kz = (int)(e % NF);
+        const int j = (int)(ij % N), i = (int)(ij / N);
+        const int kx = kof<N>(i), ky = kof<N>(j);
+        double2 d = make_double2(0.0, 0.0);
+        if (kz <= G::KC && kx * kx + ky * ky + kz * kz <= G::KC2) {
+            const cx<T> v = U[c * G::FS + ij * G::NZP + kz];
+            d = make_double2((double)v.x, (double)v.y);
+        }
+        ref[u] = d;
+    }
+}
+
 // real [6][N][N][N] (u then w) -> reference real layout [N][N][N+2][3] x2
 template <typename T, int N>
 __global__ void k_real_unpack(const T* __restrict__ R, double* __restrict__ u, double* __restrict__ w) {

@@ -239,6 +239,13 @@ ns3d_status ns3d_last_step_ms(ns3d_ctx* ctx, float* ms);
  * names[i] / ms[i] for i < *count (max_count entries at most). */
 ns3d_status ns3d_profile_step(ns3d_ctx* ctx, int reps, const char** names, float* ms,
                               double* bytes, int max_count, int* count);
+/* Bytes that crossed the host link in the last upload (host -> device) and
+ * download (device -> host) of a host array. With pinned (page-locked) host
+ * arrays the kernels read only the dealiased modes and write only the
+ * 128-byte lines that hold them, while host threads zero the rest of the
+ * output array during the step; other host memory goes through a full-size
+ * staged copy. */
+ns3d_status ns3d_io_bytes(ns3d_ctx* ctx, long long* h2d, long long* d2h);
 
 #ifdef __cplusplus
 }
