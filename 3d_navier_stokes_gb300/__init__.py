@@ -47,6 +47,8 @@ EXPORTS = (
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
     "ns3d_les_infer_host", "ns3d_les_profile_infer", "ns3d_io_bytes",
+    "ns3d_autotune", "ns3d_autotune_ensemble", "ns3d_tuning_get", "ns3d_tuning_set", "ns3d_tuning_clear", "ns3d_tuning_save",
+    "ns3d_tuning_load",
 )
 
 
@@ -71,6 +73,20 @@ class Params(ctypes.Structure):
         ("device", ctypes.c_int),
         ("stream", ctypes.c_void_p),
     ]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [
+        ("N", ctypes.c_int),
+        ("precision", ctypes.c_int),
+        ("variant", ctypes.c_int),
+        ("zform", ctypes.c_int),
+        ("ms_per_step", ctypes.c_float),
+    ]
+
+    def as_dict(self):
+        return {"N": self.N, "precision": "fp32" if self.precision == FP32 else "fp64", "variant": self.variant,
+                "zform": self.zform, "ms_per_step": self.ms_per_step}
 
 
 class Measures(ctypes.Structure):
@@ -141,6 +157,22 @@ def lib():
         L.ns3d_set_dp_tolerances.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.ns3d_dp_stats.restype = I
         L.ns3d_dp_stats.argtypes = [P, D, ctypes.POINTER(ctypes.c_long)]
+        L.ns3d_autotune.restype = I
+        L.ns3d_autotune.argtypes = [ctypes.POINTER(Params), I, ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), I,
+                                    ctypes.POINTER(ctypes.c_int)]
+        L.ns3d_autotune_ensemble.restype = I
+        L.ns3d_autotune_ensemble.argtypes = [ctypes.POINTER(Params), I, I, ctypes.POINTER(Tuning), I,
+                                             ctypes.POINTER(ctypes.c_int)]
+        L.ns3d_tuning_get.restype = I
+        L.ns3d_tuning_get.argtypes = [I, I, ctypes.POINTER(Tuning)]
+        L.ns3d_tuning_set.restype = I
+        L.ns3d_tuning_set.argtypes = [ctypes.POINTER(Tuning)]
+        L.ns3d_tuning_clear.restype = I
+        L.ns3d_tuning_clear.argtypes = []
+        L.ns3d_tuning_save.restype = I
+        L.ns3d_tuning_save.argtypes = [ctypes.c_char_p]
+        L.ns3d_tuning_load.restype = I
+        L.ns3d_tuning_load.argtypes = [ctypes.c_char_p]
         L.ns3d_io_bytes.restype = I
         L.ns3d_io_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
         L.ns3d_stream.restype = P
@@ -222,6 +254,60 @@ def _dp(a: np.ndarray):
         return None
     assert a.flags["C_CONTIGUOUS"]
     return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def autotune(N: int, steps: int = 10, **kw):
+    """Time every compiled shape (tile variant x z-pass form) of grid size N on the
+    Solver configuration kw (precision, nu, dt, cfl, ...) and keep the fastest for
+    the engines built afterwards. Returns (best, tried) as dicts."""
+    p = _params(N, **kw)
+    best = Tuning()
+    tried = (Tuning * 16)()
+    n = ctypes.c_int()
+    st = lib().ns3d_autotune(ctypes.byref(p), steps, ctypes.byref(best), tried, 16, ctypes.byref(n))
+    if st != OK:
+        raise NS3DError(st, f"ns3d_autotune(N={N}): {lib().ns3d_status_string(st).decode()}")
+    return best.as_dict(), [tried[i].as_dict() for i in range(n.value)]
+
+
+def autotune_ensemble(members, steps: int = 10):
+    """Tune every (N, precision) group of an ensemble (list of Solver keyword dicts)
+    with all of its members; returns the chosen shape per group."""
+    arr = (Params * len(members))(*[_params(**m) for m in members])
+    best = (Tuning * 16)()
+    n = ctypes.c_int()
+    st = lib().ns3d_autotune_ensemble(arr, len(members), steps, best, 16, ctypes.byref(n))
+    if st != OK:
+        raise NS3DError(st, f"ns3d_autotune_ensemble: {lib().ns3d_status_string(st).decode()}")
+    return [best[i].as_dict() for i in range(n.value)]
+
+
+def tuning(N: int, precision: str = "fp32"):
+    """The tuning-table entry of (N, precision), or None."""
+    t = Tuning()
+    st = lib().ns3d_tuning_get(N, {"fp64": FP64, "fp32": FP32}[precision], ctypes.byref(t))
+    return t.as_dict() if st == OK else None
+
+
+def tuning_set(N: int, variant: int, zform: int = 0, precision: str = "fp32"):
+    t = Tuning(N, {"fp64": FP64, "fp32": FP32}[precision], variant, zform, 0.0)
+    st = lib().ns3d_tuning_set(ctypes.byref(t))
+    if st != OK:
+        raise NS3DError(st, "ns3d_tuning_set")
+
+
+def tuning_clear():
+    lib().ns3d_tuning_clear()
+
+
+def tuning_save(path: str):
+    if lib().ns3d_tuning_save(str(path).encode()) != OK:
+        raise NS3DError(ERR_INVALID, f"ns3d_tuning_save({path})")
+
+
+def tuning_load(path: str):
+    if lib().ns3d_tuning_load(str(path).encode()) != OK:
+        raise NS3DError(ERR_INVALID, f"ns3d_tuning_load({path})")
 
 
 def n_spect(N: int) -> int:

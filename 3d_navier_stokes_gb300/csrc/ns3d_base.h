@@ -60,6 +60,10 @@ class Base {
     virtual ns3d_status les_counters(long* on, long* off) = 0;
     virtual const float* real_velocity_f32(ns3d_status* st) = 0;
     virtual ns3d_status set_state_real_host(const double* u) = 0;
+    // z-pass form: 0 the persistent line kernel where compiled, 1 the CTA-synchronous pass
+    virtual void set_zform(int z) = 0;
+    virtual int zform() const = 0;
+    virtual int variant() const = 0;
 
     const char* err() const { return err_; }
     void set_err(const char* fmt, ...) {
@@ -76,11 +80,20 @@ class Base {
     char err_[512];
 };
 
-// Factories, one per precision (ns3d_inst_f32.cu / ns3d_inst_f64.cu): an
-// engine for M members of grid size N with parameters ps[0..M-1].
+// Factories, one per precision (ns3d_tune.cu): an engine for M members of
+// grid size N with parameters ps[0..M-1], built with the tile variant and
+// z-pass form the tuning table holds for (N, precision).
 Base* make_f32(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f64(int N, const ns3d_params* ps, int M, cudaStream_t s);
+// one compiled tile variant (nullptr where that variant is not compiled for N)
+Base* make_f32_v0(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v1(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v2(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v3(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v4(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f64_v0(int N, const ns3d_params* ps, int M, cudaStream_t s);
 bool supported_n(int N);
+constexpr int kTileVariants = 5;   // TileVar<0..4>, PlansV (ns3d_kernels.cuh)
 
 inline unsigned long long host_splitmix64(unsigned long long x) {
     unsigned long long z = x + 0x9E3779B97F4A7C15ull;

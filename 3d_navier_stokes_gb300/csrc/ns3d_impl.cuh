@@ -32,13 +32,13 @@ namespace ns3d {
 // e^{-2 pi i m / n} with the quarter-turn reduction used by the transforms.
 void twiddle_table(int n, double* re, double* im);
 
-template <typename T, int N>
+template <typename T, int N, int V = 0>
 class Impl final : public Base {
     using G = Geo<N>;
     using PA = typename Plans<N>::A;
-    using PX = typename Plans<N>::X;
-    static constexpr int TA = tile_a<T, N>();
-    static constexpr int TX = tile_x<T, N>();
+    using PX = typename PlansV<N, V>::X;
+    static constexpr int TA = tile_a<T, N, V>();
+    static constexpr int TX = tile_x<T, N, V>();
     static constexpr int ZP = zpairs<N>();
     static constexpr int NTA = (G::NZ1 + TA - 1) / TA;
     static constexpr int NTX = (G::NZ1 + TX - 1) / TX;
@@ -125,9 +125,9 @@ class Impl final : public Base {
         }
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
         // opt-in shared memory sizes
-        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x()));
-        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
-        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x()));
+        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         if constexpr (zline_ok<T, N>()) {
             NS3D_CK(cudaFuncSetAttribute(k_zline<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_zl()));
@@ -141,7 +141,7 @@ class Impl final : public Base {
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
-        NS3D_CK(cudaFuncSetAttribute(k_xfwd<T, N, INT_TAB, X_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        NS3D_CK(cudaFuncSetAttribute(k_xfwd<T, N, INT_TAB, X_STAGE1, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      smem_x()));
         tables(0, 0, M_);
         NS3D_CK(cudaGetLastError());
@@ -158,46 +158,59 @@ class Impl final : public Base {
 
     template <int INTEG>
     void set_xfwd_attrs() {
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE3>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE4>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_RHS>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
-        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_PLAIN>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE1, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE2, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE3, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE4, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_RHS, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
+        cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_PLAIN, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
     }
 
     // each launcher covers members [m0, m0 + cnt); `in` points at member 0's arrays
     void p1(const cx<T>* in, int m0, int cnt) {
-        k_xinv<T, N><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
+        k_xinv<T, N, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
     }
     void p2(int m0, int cnt) {
-        k_ypass<T, N, true><<<dim3(NTA, N, 6 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+        k_ypass<T, N, true, V><<<dim3(NTA, N, 6 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
     }
     static constexpr size_t smem_zl() { return zline_smem<T, N>(); }
     void p3(int want_umax, int m0, int cnt) {
         if constexpr (zline_ok<T, N>()) {
-            // persistent: as many CTAs as fit on the device, never more than there are warp tasks
-            const long long groups = (long long)N * N / zline_gpw<N>() * cnt;
-            long long grid = (long long)zline_ctas_;
-            if (grid * ZLINE_WARPS > groups) grid = (groups + ZLINE_WARPS - 1) / ZLINE_WARPS;
-            k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(Wm(m0), tw_, sdm(m0), want_umax, cnt);
-        } else {
-            k_zpass<T, N, 0><<<dim3((unsigned)((long long)N * N / 2 / ZP), cnt), 3 * PA::P * ZP, smem_z(), s_>>>(
-                Wm(m0), tw_, nullptr, sdm(m0), want_umax);
+            if (zform_ == 0) {
+                // persistent: as many CTAs as fit on the device, never more than there are warp tasks
+                const long long groups = (long long)N * N / zline_gpw<N>() * cnt;
+                long long grid = (long long)zline_ctas_;
+                if (grid * ZLINE_WARPS > groups) grid = (groups + ZLINE_WARPS - 1) / ZLINE_WARPS;
+                k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(Wm(m0), tw_, sdm(m0), want_umax,
+                                                                                   cnt);
+                return;
+            }
         }
+        k_zpass<T, N, 0><<<dim3((unsigned)((long long)N * N / 2 / ZP), cnt), 3 * PA::P * ZP, smem_z(), s_>>>(
+            Wm(m0), tw_, nullptr, sdm(m0), want_umax);
     }
+    void set_zform(int z) override {
+        const int zn = (zline_ok<T, N>() && z == 0) ? 0 : 1;
+        if (zn != zform_ && graph_exec_) {
+            cudaGraphExecDestroy(graph_exec_);
+            graph_exec_ = nullptr;
+        }
+        zform_ = zn;
+    }
+    int zform() const override { return zform_; }
+    int variant() const override { return V; }
     void p4(int m0, int cnt) {
-        k_ypass<T, N, false><<<dim3(NTA, N, 3 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+        k_ypass<T, N, false, V><<<dim3(NTA, N, 3 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
     }
     template <int INTEG, int MODE>
     void p5x(int m0, int cnt, cx<T>* out) {
-        k_xfwd<T, N, INTEG, MODE><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+        k_xfwd<T, N, INTEG, MODE, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
             Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0),
             (les_ && MODE <= X_STAGE4) ? F_ : nullptr, nullptr, nullptr, RkStage{});
     }
     // RK5-family stage epilogue s (0-based) of members [m0, m0 + cnt)
     void p5tab(int s, int m0, int cnt) {
-        k_xfwd<T, N, INT_TAB, X_STAGE1><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+        k_xfwd<T, N, INT_TAB, X_STAGE1, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
             Wm(m0), Um(m0), UTm(m0), ACCm(m0), tw_, sdm(m0), tabm(m0), les_ ? F_ : nullptr,
             K_ + (size_t)m0 * 18 * G::FS, dpart_ + (size_t)m0 * 3 * NTX * G::NKY, rk_stage(s, dp5()));
     }
@@ -225,7 +238,7 @@ class Impl final : public Base {
             k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
                 W_, tw_, tau_real_ + h * 3 * M3, nullptr, 0);
             p4(0, 1);
-            k_xfwd<T, N, INT_IFRK4, X_PLAIN><<<dim3(NTX, G::NKY, 1), TX * PX::P, smem_x(), s_>>>(
+            k_xfwd<T, N, INT_IFRK4, X_PLAIN, V><<<dim3(NTX, G::NKY, 1), TX * PX::P, smem_x(), s_>>>(
                 W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr, nullptr, nullptr, RkStage{});
         }
         k_sgs_div<T, N><<<kSgsParts, 256, 0, s_>>>(TAU_, U_, F_, sgs_part_);
@@ -391,7 +404,8 @@ class Impl final : public Base {
             set_err("per-kernel profile covers the RK4-family step");
             return NS3D_ERR_UNSUPPORTED;
         }
-        static const char* kNames[6] = {"k_xinv", "k_ypass_inv", zline_ok<T, N>() ? "k_zline" : "k_zpass", "k_ypass_fwd", "k_xfwd", "k_misc"};
+        const char* kNames[6] = {"k_xinv", "k_ypass_inv", zform_ == 0 ? "k_zline" : "k_zpass", "k_ypass_fwd", "k_xfwd",
+                                 "k_misc"};
         std::vector<cudaEvent_t> ev(2 * 6 * 4 + 2);
         for (auto& e : ev) NS3D_CK(cudaEventCreate(&e));
         double acc[6] = {0, 0, 0, 0, 0, 0};
@@ -908,6 +922,7 @@ class Impl final : public Base {
     cudaGraphExec_t graph_exec_ = nullptr;
     cudaEvent_t ev0_ = nullptr, ev1_ = nullptr;
     int zline_ctas_ = 1;
+    int zform_ = zline_ok<T, N>() ? 0 : 1;
     LesHook* les_ = nullptr;       // learned closure (single FP32 run)
     cx<T>* TAU_ = nullptr;         // tau_ij spectra (6 fields)
     cx<T>* F_ = nullptr;           // -div(tau) (3 fields)

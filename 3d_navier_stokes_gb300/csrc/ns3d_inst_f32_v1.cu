@@ -1,0 +1,15 @@
+// ns3d_inst_f32_v1.cu — FP32-bulk engines in tile variant 1 (TileVar<1>) for
+// the sizes the autotuner chooses among.
+#include "ns3d_inst.cuh"
+
+namespace ns3d {
+Base* make_f32_v1(int N, const ns3d_params* ps, int M, cudaStream_t s) {
+    using T = float;
+    constexpr int V = 1;
+    switch (N) {
+        NS3D_TUNED_SIZES(NS3D_CASE)
+        default:
+            return nullptr;
+    }
+}
+}  // namespace ns3d

@@ -25,6 +25,8 @@
 // velocity/vorticity and the forward transform yields the reference's
 // FFT(u x w)/N^6 directly.
 #pragma once
+#include <type_traits>
+
 #include "fft_engine.cuh"
 #include "tma.cuh"
 
@@ -62,21 +64,42 @@ template <> struct Plans<512>  { using A = Plan<512, 16, 8, 8, 8>;   using X = P
 template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = Plan<1024, 8, 8, 8, 4, 4>; };
 
 // Tile width (pencils per CTA along kz) of the strided passes: one 128-byte
-// row segment per pencil row where the thread count allows.
+// row segment per pencil row where the thread count allows. Variant V of the
+// FP32 engines asks for other widths (clipped to 512 threads per CTA); the
+// autotuner times the compiled variants of a grid size and keeps the fastest.
 #ifndef NS3D_TILE_A32
 #define NS3D_TILE_A32 8
 #endif
 #ifndef NS3D_TILE_X32
 #define NS3D_TILE_X32 16
 #endif
-template <typename T, int N> constexpr int tile_a() {
-    return sizeof(T) == 4 ? (Plans<N>::A::P * NS3D_TILE_A32 <= 512 ? NS3D_TILE_A32 : 8)
-                          : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
+template <int V> struct TileVar;
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32; };
+template <> struct TileVar<1> { static constexpr int A = 4, X = 8; };
+template <> struct TileVar<2> { static constexpr int A = 16, X = 8; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 8; };
+
+// Plans of variant V: variants 3 and 4 give the x passes a plan with twice
+// the elements per thread (half the threads per pencil), with 16 pencils per
+// CTA (every row access a full 128-byte segment) or 8 (more registers per
+// thread at the largest sizes).
+template <int N> struct AltX { using X = typename Plans<N>::X; };
+template <> struct AltX<64> { using X = Plan<64, 16, 16, 4>; };
+template <> struct AltX<128> { using X = Plan<128, 16, 16, 8>; };
+template <> struct AltX<256> { using X = Plan<256, 16, 16, 16>; };
+template <> struct AltX<512> { using X = Plan<512, 16, 8, 8, 8>; };
+template <int N, int V> struct PlansV {
+    using A = typename Plans<N>::A;
+    using X = typename std::conditional<(V >= 3), typename AltX<N>::X, typename Plans<N>::X>::type;
+};
+template <int P, int W> constexpr int clip_tile() { return P * W <= 512 ? W : (P * 8 <= 512 ? 8 : (P * 4 <= 512 ? 4 : 2)); }
+template <typename T, int N, int V = 0> constexpr int tile_a() {
+    return sizeof(T) == 4 ? clip_tile<Plans<N>::A::P, TileVar<V>::A>() : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
 }
-template <typename T, int N> constexpr int tile_x() {
-    constexpr int P = Plans<N>::X::P;
-    return sizeof(T) == 4 ? (P * NS3D_TILE_X32 <= 512 ? NS3D_TILE_X32 : (P * 8 <= 512 ? 8 : 4))
-                          : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
+template <typename T, int N, int V = 0> constexpr int tile_x() {
+    constexpr int P = PlansV<N, V>::X::P;
+    return sizeof(T) == 4 ? clip_tile<P, TileVar<V>::X>() : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
 }
 // line pairs per CTA of the z pass (>= 96 threads)
 template <int N> constexpr int zpairs() {
@@ -144,12 +167,12 @@ enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAI
 // are loaded up front; the kx-weighted inputs of the vorticity are formed in
 // registers, so the five transforms below read each input once.
 // ---------------------------------------------------------------------------
-template <typename T, int N>
-__global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
+template <typename T, int N, int V = 0>
+__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P)
 k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
-    using PL = typename Plans<N>::X;
-    constexpr int TT = tile_x<T, N>();
+    using PL = typename PlansV<N, V>::X;
+    constexpr int TT = tile_x<T, N, V>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -223,12 +246,12 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // Inverse: inputs only where ky^2 + kz^2 <= KC^2, outputs every y.
 // Forward: inputs every y, outputs only where ky^2 + kz^2 <= KC^2.
 // ---------------------------------------------------------------------------
-template <typename T, int N, bool INV>
-__global__ void __launch_bounds__(tile_a<T, N>() * Plans<N>::A::P)
+template <typename T, int N, bool INV, int V = 0>
+__global__ void __launch_bounds__(tile_a<T, N, V>() * Plans<N>::A::P)
 k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
-    constexpr int TT = tile_a<T, N>();
+    constexpr int TT = tile_a<T, N, V>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);
@@ -608,15 +631,15 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
 // T. INTEG = INT_TAB runs the RkStage epilogue of the RK5 family; its DP5CN
 // error partial sums go to dpart[member][block][3] in a fixed order.
 // ---------------------------------------------------------------------------
-template <typename T, int N, int INTEG, int MODE>
-__global__ void __launch_bounds__(tile_x<T, N>() * Plans<N>::X::P)
+template <typename T, int N, int INTEG, int MODE, int V = 0>
+__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P)
 k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
        cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
        const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs, cx<T>* __restrict__ K,
        double* __restrict__ dpart, const RkStage rs) {
     using G = Geo<N>;
-    using PL = typename Plans<N>::X;
-    constexpr int TT = tile_x<T, N>();
+    using PL = typename PlansV<N, V>::X;
+    constexpr int TT = tile_x<T, N, V>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);

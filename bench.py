@@ -44,6 +44,7 @@ def parse():
     ap.add_argument("--N", type=int, default=512)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256"])
     ap.add_argument("--snapshots", type=int, default=2000)
@@ -216,7 +217,12 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     dist = Dist(ws, rank, local, True)
     N = args.N
-    s = pkg.Solver(N, nu=1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    cfg = dict(nu=1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    tuned = None
+    if not args.no_autotune:
+        # the library's autotuner picks the tile / radix variant and z-pass form of this size (untimed)
+        tuned, _ = pkg.autotune(N, steps=10, **cfg)
+    s = pkg.Solver(N, **cfg)
     s.InitialConditions("SPECTRUM", seed=0, k0=4.0, energy=1.0)
     stream = torch.cuda.ExternalStream(s.stream)
     s.RK4Step(args.warmup)
@@ -302,7 +308,7 @@ def run_ours(args, ws, rank, local):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(WORKLOAD, N=N, parallelism=f"replicas x{ws}"),
+            "config": dict(WORKLOAD, N=N, parallelism=f"replicas x{ws}", autotune=tuned),
             "clocks": clocks, "e2e": e2e, "gpu_launches": s_kernels(pkg, N) * args.steps,
             "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
             "library_ms_per_step": lib_ms / args.steps,
@@ -332,6 +338,10 @@ def run_ensemble(args, local):
     k0 = rng.uniform(2.0, 6.0, len(sizes))
     nu = np.exp(rng.uniform(np.log(5e-4), np.log(5e-3), len(sizes)))
     members = [dict(N=n, nu=float(v), dt=1e-3, cfl=0.5, precision="fp32", device=local) for n, v in zip(sizes, nu)]
+    # autotuner: tile variant and z-pass form per grid size, timed with each size's members
+    t0 = time.perf_counter()
+    tuned = pkg.autotune_ensemble(members, steps=10)
+    tune_s = time.perf_counter() - t0
     ens = pkg.Ensemble(members)
     for i in range(len(sizes)):
         ens.InitialConditions(i, "SPECTRUM", seed=i, k0=float(k0[i]))
@@ -351,6 +361,7 @@ def run_ensemble(args, local):
             "config": {"workload": "batched ensemble, FP32, IF-RK4, CFL 0.5, one graph launch per step",
                        "members": len(sizes), "launch_groups": groups, "grid_points": pts},
             "clocks": clocks, "gpu_launches": kps * args.steps,
+            "autotune": {"seconds": tune_s, "choices": tuned},
             "energy_samples": e0}
     print(json.dumps(line), flush=True)
     ens.close()

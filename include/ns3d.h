@@ -229,6 +229,36 @@ ns3d_status ns3d_les_attach(ns3d_ctx* coarse, ns3d_les* l);
 /* steps taken with the closure and steps that fell back to the plain solve */
 ns3d_status ns3d_les_counters(ns3d_ctx* coarse, long* closure_steps, long* fallback_steps);
 
+/* ------------------------------------------------------------------------
+ * Autotuner. An FP32 engine of a grid size exists in several compiled shapes:
+ * tile variants 0..2 (pencils per CTA of the strided x and y FFT passes) and
+ * two z-pass forms (0: persistent bulk-copy line kernel, 1: CTA-synchronous
+ * pass). ns3d_autotune times every shape of params->N / params->precision on
+ * the configuration *params (SPECTRUM initial condition, k0 = 4, seed 0;
+ * 3 warm-up steps, then `steps` timed steps) and keeps the fastest in a
+ * process-wide table; ns3d_create and ns3d_ensemble_create then build engines
+ * of that (N, precision) in the chosen shape. The table can be saved to and
+ * loaded from a text file; the environment variable NS3D_TUNING_FILE names a
+ * file loaded before the first engine is built. */
+typedef struct {
+    int   N;
+    int   precision;    /* ns3d_precision                          */
+    int   variant;      /* tile variant                            */
+    int   zform;        /* z-pass form                             */
+    float ms_per_step;  /* timed device milliseconds per step      */
+} ns3d_tuning;
+ns3d_status ns3d_autotune(const ns3d_params* params, int steps, ns3d_tuning* best, ns3d_tuning* tried,
+                          int max_tried, int* n_tried);
+/* the same for an ensemble: every (N, precision) group of `members` is timed
+ * with all of its members in each shape; one best entry per group */
+ns3d_status ns3d_autotune_ensemble(const ns3d_params* members, int count, int steps, ns3d_tuning* best,
+                                   int max_best, int* n_best);
+ns3d_status ns3d_tuning_get(int N, int precision, ns3d_tuning* t);   /* NS3D_ERR_INVALID: no entry */
+ns3d_status ns3d_tuning_set(const ns3d_tuning* t);
+ns3d_status ns3d_tuning_clear(void);
+ns3d_status ns3d_tuning_save(const char* path);
+ns3d_status ns3d_tuning_load(const char* path);
+
 /* Instrumentation for benchmarks: the stream the context runs on, the number
  * of kernels one step launches, and the device time of the last ns3d_step
  * call (CUDA events on the context stream), in milliseconds. */

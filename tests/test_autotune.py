@@ -1,0 +1,68 @@
+"""Autotuner (ns3d_autotune / ns3d_tuning_*): every compiled shape of a grid
+size (tile / radix variant x z-pass form) is timed and the fastest kept;
+engines built afterwards use it."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def run(ns3d, N, steps=5):
+    s = ns3d.Solver(N, nu=0.005, dt=1e-3, precision="fp32")
+    s.InitialConditions("SPECTRUM", seed=2, k0=4.0)
+    s.RK4Step(steps)
+    return s.get_state()
+
+
+@pytest.mark.parametrize("N", [48, 64, 128])
+def test_tile_variants_are_bit_identical(ns3d, N):
+    """Variants 1 and 2 change only the pencils per CTA: bit-identical. Variant 3
+    (another x-pass radix plan, where compiled; variant 4 the same plan in other
+    tiles) and the z-pass forms change the
+    order of the butterflies: FP32 rounding."""
+    states = {}
+    for v in range(5):
+        for z in (0, 1):
+            ns3d.tuning_set(N, v, z)
+            states[(v, z)] = run(ns3d, N)
+    ns3d.tuning_clear()
+    for v in (1, 2):
+        assert np.array_equal(states[(v, 0)], states[(0, 0)])
+        assert np.array_equal(states[(v, 1)], states[(0, 1)])
+    assert np.array_equal(states[(4, 0)], states[(3, 0)])   # same x plan, other tiles
+    ref = states[(0, 0)]
+    for key in ((0, 1), (3, 0), (3, 1)):
+        assert np.linalg.norm(states[key] - ref) < 1e-6 * np.linalg.norm(ref), key
+
+
+def test_autotune_picks_fastest_and_persists(ns3d, tmp_path):
+    ns3d.tuning_clear()
+    best, tried = ns3d.autotune(64, steps=10, precision="fp32", nu=0.005, dt=1e-3)
+    assert len(tried) == 10   # 5 variants x 2 z-pass forms at 64^3
+    assert best["ms_per_step"] == min(t["ms_per_step"] for t in tried)
+    assert ns3d.tuning(64) == best
+    f = tmp_path / "tune.txt"
+    ns3d.tuning_save(f)
+    ns3d.tuning_clear()
+    assert ns3d.tuning(64) is None
+    ns3d.tuning_load(f)
+    got = ns3d.tuning(64)
+    assert (got["variant"], got["zform"]) == (best["variant"], best["zform"])
+    # an ensemble built now uses the tuned shape and still equals single runs
+    members = [dict(N=64, nu=0.005, dt=1e-3, precision="fp32"), dict(N=64, nu=0.002, dt=1e-3, precision="fp32")]
+    ens = ns3d.Ensemble(members)
+    for m in range(2):
+        ens.InitialConditions(m, "SPECTRUM", seed=m + 4, k0=3.0)
+    ens.step(3)
+    for m, kw in enumerate(members):
+        s = ns3d.Solver(**kw)
+        s.InitialConditions("SPECTRUM", seed=m + 4, k0=3.0)
+        s.RK4Step(3)
+        assert np.array_equal(ens.get_state(m), s.get_state())
+    ns3d.tuning_clear()
+
+
+def test_fp64_has_one_shape(ns3d):
+    best, tried = ns3d.autotune(32, steps=3, precision="fp64", nu=0.01, dt=1e-3)
+    assert len(tried) == 1 and best["zform"] == 1
+    ns3d.tuning_clear()
