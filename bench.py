@@ -45,8 +45,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256"])
+    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256", "closure-infer"])
     ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
     ap.add_argument("--les-steps", type=int, default=2000)
@@ -217,7 +218,9 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     dist = Dist(ws, rank, local, True)
     N = args.N
-    cfg = dict(nu=1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    # nu = 1e-3 at 512^3; the 1024^3 variant of the configuration runs nu = 4e-4
+    cfg = dict(nu=4e-4 if N >= 1024 else 1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2,
+               device=local)
     tuned = None
     if not args.no_autotune:
         # the library's autotuner picks the tile / radix variant and z-pass form of this size (untimed)
@@ -261,30 +264,31 @@ def run_ours(args, ws, rank, local):
     roofline["step_compulsory_GB"] = step_bytes / 1e9
     roofline["step_survey_model_GBps"] = survey_bytes / (ms_max / args.steps / 1e3) / 1e9
 
-    # e2e: RK4Step's host-array contract through the C ABI (pinned host buffers,
-    # H2D of u_hat, one step, D2H of u_hat, every step)
-    fshape = (N, N, N // 2 + 1, 3)
-    hin = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
-    hout = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
-    hin[...] = s.get_state()
-    s.step_host(hin, hout)   # warm
-    ke = max(1, args.e2e_steps)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(ke):
-        s.step_host(hin, hout)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e2e_ms = dist.max(e0.elapsed_time(e1))
-    nbytes = int(np.prod(fshape)) * 16
-    h2d, d2h = s.io_bytes()   # bytes that crossed the host link per call (dealiased modes / their lines)
-    e2e = {"value": ws * N ** 3 * ke / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
-           "d2h_bytes_per_step": d2h, "host_array_bytes": nbytes, "steps": ke,
-           "call": "ns3d_step_host(ctx, u_hat_in, u_hat_out), reference layout complex128[N][N][N/2+1][3], "
-                   "pinned host arrays"}
+    e2e = None
+    if not args.no_e2e:
+        # e2e: RK4Step's host-array contract through the C ABI (pinned host buffers,
+        # H2D of u_hat, one step, D2H of u_hat, every step)
+        fshape = (N, N, N // 2 + 1, 3)
+        hin = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+        hout = torch.empty(fshape + (2,), dtype=torch.float64, pin_memory=True).numpy().view(np.complex128)[..., 0]
+        hin[...] = s.get_state()
+        s.step_host(hin, hout)   # warm
+        ke = max(1, args.e2e_steps)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(ke):
+            s.step_host(hin, hout)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        e2e_ms = dist.max(e0.elapsed_time(e1))
+        nbytes = int(np.prod(fshape)) * 16
+        h2d, d2h = s.io_bytes()   # bytes that crossed the host link per call (dealiased modes / their lines)
+        e2e = {"value": ws * N ** 3 * ke / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "host_array_bytes": nbytes, "steps": ke,
+               "call": "ns3d_step_host(ctx, u_hat_in, u_hat_out), reference layout complex128[N][N][N/2+1][3], "
+                       "pinned host arrays"}
     s.close()
-    del hin, hout
 
     fp64 = None
     if not args.no_fp64:
@@ -432,6 +436,28 @@ def run_les(args, local):
     les.close()
 
 
+def run_closure_infer(args, local):
+    """Closure inference alone: the 4-layer network on a 64^3 grid (tensor-core path), random
+    weights and input, mean device time of --steps calls after --warmup."""
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    D = 64
+    les = pkg.LES(D, capacity=0, seed=1)
+    u = np.random.default_rng(0).standard_normal((3, D, D, D)).astype(np.float32)
+    tau = les.infer(u)
+    les.profile_infer(max(1, args.warmup))
+    ms = les.profile_infer(max(1, args.steps))
+    flops = 126144.0 * D ** 3
+    print(json.dumps({"metric": "closure inference (64^3, 4 conv layers, tcgen05 BF16 / FP32 accumulate)",
+                      "value": ms, "unit": "ms", "higher_is_better": False, "tflops": flops / (ms * 1e-3) / 1e12,
+                      "steps": args.steps, "finite": bool(np.isfinite(tau).all())}), flush=True)
+    les.close()
+
+
 def run_decay(args, local):
     """Config C2: decaying turbulence at 256^3 (SPECTRUM IC k0 = 4, nu = 2e-3, CFL 0.5, IF-RK4,
     --decay-steps steps) in FP64 and in FP32; reports the FP32 relative errors of the energy, the
@@ -480,6 +506,9 @@ def main():
         return
     if args.workload == "decay256":
         run_decay(args, local)
+        return
+    if args.workload == "closure-infer":
+        run_closure_infer(args, local)
         return
     run_ours(args, ws, rank, local)
 
