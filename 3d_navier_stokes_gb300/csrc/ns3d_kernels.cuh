@@ -468,10 +468,19 @@ constexpr bool zline_ok() {
            ((long long)N * N) % (32 / Plans<N>::A::P) == 0;
 }
 template <int N> constexpr int zline_gpw() { return 32 / Plans<N>::A::P; }
-// complex elements of shared memory per warp: 2 stages x GPW lines x 6 fields x NZP, plus the
-// GPW exchange buffers, rounded up to 16 elements
+// With several lines per warp (N <= 256) the exchange buffers live in the
+// stage buffer whose lines are already in registers, which cuts shared memory
+// per warp by a fifth (3 CTAs per SM instead of 2 at 168 registers); a
+// 512-point line (32 lanes x 16 elements, over 200 registers) keeps its own.
+template <int N> constexpr bool zline_xbuf_in_stage() { return zline_gpw<N>() > 1; }
+template <int N> constexpr int zline_stage_elems() {
+    constexpr int a = zline_gpw<N>() * 6 * Geo<N>::NZP, b = zline_gpw<N>() * zpad<N>();
+    return ((zline_xbuf_in_stage<N>() && b > a ? b : a) + 15) / 16 * 16;
+}
+// complex elements of shared memory per warp: two stage buffers (+ the exchange buffers)
 template <typename T, int N> constexpr int zline_warp_elems() {
-    return (2 * zline_gpw<N>() * 6 * Geo<N>::NZP + zline_gpw<N>() * zpad<N>() + 15) / 16 * 16;
+    return 2 * zline_stage_elems<N>() +
+           (zline_xbuf_in_stage<N>() ? 0 : (zline_gpw<N>() * zpad<N>() + 15) / 16 * 16);
 }
 template <typename T, int N> constexpr size_t zline_smem() {
     return sizeof(cx<T>) * (size_t)ZLINE_WARPS * zline_warp_elems<T, N>() + 16 * ZLINE_WARPS;
@@ -486,15 +495,14 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
     constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>();
     constexpr int NZP = G::NZP;
     constexpr long long NG = (long long)N * N / GPW;   // line groups per ensemble member
-    constexpr int SE = GPW * 6 * NZP;                  // elements per stage
-    constexpr uint32_t STAGE_BYTES = SE * sizeof(cx<T>);
+    constexpr int SE = zline_stage_elems<N>();         // elements per stage buffer
+    constexpr uint32_t STAGE_BYTES = GPW * 6 * NZP * sizeof(cx<T>);   // bytes copied per stage
     constexpr uint32_t LINE_BYTES = NZP * sizeof(cx<T>);
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int p = lane % P, gi = lane / P;
     cx<T>* wbase = reinterpret_cast<cx<T>*>(smem_raw) + (size_t)warp * zline_warp_elems<T, N>();
     cx<T>* stage[2] = {wbase, wbase + SE};
-    cx<T>* sb = wbase + 2 * SE + gi * zpad<N>();
     uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + sizeof(cx<T>) * (size_t)ZLINE_WARPS *
                                                                 zline_warp_elems<T, N>()) + 2 * warp;
     PaddedIdx sidx;
@@ -553,6 +561,8 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         cx<T>* Wm = W + mem * 6 * G::FS;
         const cx<T>* in = stage[s] + gi * 6 * NZP;
         const long long line = (g % NG) * GPW + gi;
+        // exchange buffer of this group (in the stage buffer once its lines are in registers)
+        cx<T>* sb = (zline_xbuf_in_stage<N>() ? stage[s] : wbase + 2 * SE) + gi * zpad<N>();
 
         auto load_pair = [&](int f, cx<T>(&v)[E]) {
             const cx<T>* A = in + f * NZP;
@@ -578,6 +588,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         load_pair(0, V1);
         load_pair(2, V2);
         load_pair(4, V3);
+        __syncwarp();   // every lane has read the staged lines before the buffer is reused
         PL::inv(V1, sb, p, tw, sidx, sync);
         PL::inv(V2, sb, p, tw, sidx, sync);
         PL::inv(V3, sb, p, tw, sidx, sync);
@@ -619,6 +630,9 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
             const int m = p + P * q;
             if (m <= G::KC) outC[m] = V2[q];
         }
+        // the stage buffer is refilled by a bulk copy (async proxy) next iteration:
+        // order every lane's exchange accesses to it before that
+        fence_proxy_async_smem();
         __syncwarp();
     }
     flush_umax();
