@@ -177,10 +177,11 @@ class Impl final : public Base {
     void p3(int want_umax, int m0, int cnt) {
         if constexpr (zline_ok<T, N>()) {
             if (zform_ == 0) {
-                // persistent: as many CTAs as fit on the device, never more than there are warp tasks
-                const long long groups = (long long)N * N / zline_gpw<N>() * cnt;
+                // persistent: as many CTAs as fit on the device, never more than there are line groups
+                const long long items = (long long)N * N / zline_gpw<N>() * cnt;
+                constexpr int ng = zline_groups<N>();
                 long long grid = (long long)zline_ctas_;
-                if (grid * ZLINE_WARPS > groups) grid = (groups + ZLINE_WARPS - 1) / ZLINE_WARPS;
+                if (grid * ng > items) grid = (items + ng - 1) / ng;
                 k_zline<T, N><<<(unsigned)grid, ZLINE_WARPS * 32, smem_zl(), s_>>>(Wm(m0), tw_, sdm(m0), want_umax,
                                                                                    cnt);
                 return;

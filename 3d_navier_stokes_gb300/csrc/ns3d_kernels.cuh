@@ -460,30 +460,46 @@ k_zpass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, T* __restrict__ rea
 struct SyncWarp {
     __device__ __forceinline__ void operator()() const { __syncwarp(); }
 };
+// the GW warps that share one z line: named barrier `id` over their 32 GW threads
+struct SyncGroup {
+    int id, nthreads;
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+    }
+};
 constexpr int ZLINE_WARPS = 4;
 
+// A line group is the lanes that transform one z line: P = N/E lanes. With
+// P <= 32 a warp holds 32/P lines (GPW); with P = 64 (N = 1024) two warps hold
+// one line (GW = 2) and exchange through a named barrier.
+template <int N> constexpr int zline_gw() { return Plans<N>::A::P > 32 ? Plans<N>::A::P / 32 : 1; }
+template <int N> constexpr int zline_gpw() { return Plans<N>::A::P <= 32 ? 32 / Plans<N>::A::P : 1; }
 template <typename T, int N>
 constexpr bool zline_ok() {
-    return sizeof(T) == 4 && Plans<N>::A::P <= 32 && (32 % Plans<N>::A::P) == 0 && Plans<N>::A::E <= 16 &&
-           ((long long)N * N) % (32 / Plans<N>::A::P) == 0;
+    constexpr int P = Plans<N>::A::P;
+    return sizeof(T) == 4 && Plans<N>::A::E <= 16 &&
+           (P <= 32 ? (32 % P == 0 && ((long long)N * N) % (32 / P) == 0) : P == 64);
 }
-template <int N> constexpr int zline_gpw() { return 32 / Plans<N>::A::P; }
 // With several lines per warp (N <= 256) the exchange buffers live in the
 // stage buffer whose lines are already in registers, which cuts shared memory
-// per warp by a fifth (3 CTAs per SM instead of 2 at 168 registers); a
-// 512-point line (32 lanes x 16 elements, over 200 registers) keeps its own.
+// per warp by a fifth (3 CTAs per SM instead of 2 at 168 registers); 512- and
+// 1024-point lines (16 elements per lane, over 200 registers) keep their own.
 template <int N> constexpr bool zline_xbuf_in_stage() { return zline_gpw<N>() > 1; }
 template <int N> constexpr int zline_stage_elems() {
     constexpr int a = zline_gpw<N>() * 6 * Geo<N>::NZP, b = zline_gpw<N>() * zpad<N>();
     return ((zline_xbuf_in_stage<N>() && b > a ? b : a) + 15) / 16 * 16;
 }
-// complex elements of shared memory per warp: two stage buffers (+ the exchange buffers)
-template <typename T, int N> constexpr int zline_warp_elems() {
+// complex elements of shared memory per line group: two stage buffers (+ the exchange buffers)
+template <typename T, int N> constexpr int zline_group_elems() {
     return 2 * zline_stage_elems<N>() +
            (zline_xbuf_in_stage<N>() ? 0 : (zline_gpw<N>() * zpad<N>() + 15) / 16 * 16);
 }
+// line groups per CTA
+template <int N> constexpr int zline_groups() { return ZLINE_WARPS / zline_gw<N>(); }
+// shared memory: the groups' buffers, two mbarriers per group, one vote word per warp
 template <typename T, int N> constexpr size_t zline_smem() {
-    return sizeof(cx<T>) * (size_t)ZLINE_WARPS * zline_warp_elems<T, N>() + 16 * ZLINE_WARPS;
+    return sizeof(cx<T>) * (size_t)zline_groups<N>() * zline_group_elems<T, N>() + 16 * zline_groups<N>() +
+           4 * ZLINE_WARPS;
 }
 
 template <typename T, int N>
@@ -492,30 +508,35 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         int nmem) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
-    constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>();
+    constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>(), GW = zline_gw<N>(), GT = 32 * GW;
+    constexpr int NGRP = zline_groups<N>();
     constexpr int NZP = G::NZP;
-    constexpr long long NG = (long long)N * N / GPW;   // line groups per ensemble member
+    constexpr long long NG = (long long)N * N / GPW;   // work items (line groups) per ensemble member
     constexpr int SE = zline_stage_elems<N>();         // elements per stage buffer
     constexpr uint32_t STAGE_BYTES = GPW * 6 * NZP * sizeof(cx<T>);   // bytes copied per stage
     constexpr uint32_t LINE_BYTES = NZP * sizeof(cx<T>);
     extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int p = lane % P, gi = lane / P;
-    cx<T>* wbase = reinterpret_cast<cx<T>*>(smem_raw) + (size_t)warp * zline_warp_elems<T, N>();
+    const int lane = threadIdx.x & 31;
+    const int gt = threadIdx.x % GT, grp = threadIdx.x / GT;   // thread within its line group, group
+    const int p = gt % P, gi = gt / P;
+    cx<T>* wbase = reinterpret_cast<cx<T>*>(smem_raw) + (size_t)grp * zline_group_elems<T, N>();
     cx<T>* stage[2] = {wbase, wbase + SE};
-    uint64_t* bars = reinterpret_cast<uint64_t*>(smem_raw + sizeof(cx<T>) * (size_t)ZLINE_WARPS *
-                                                                zline_warp_elems<T, N>()) + 2 * warp;
+    uint64_t* bars_all = reinterpret_cast<uint64_t*>(smem_raw + sizeof(cx<T>) * (size_t)NGRP * zline_group_elems<T, N>());
+    uint64_t* bars = bars_all + 2 * grp;
+    int* votes = reinterpret_cast<int*>(bars_all + 2 * NGRP) + grp * GW;   // one word per warp of the group
     PaddedIdx sidx;
-    SyncWarp sync;
+    using Sync = typename std::conditional<(GW > 1), SyncGroup, SyncWarp>::type;
+    Sync sync{};
+    if constexpr (GW > 1) sync = Sync{1 + grp, GT};
 
-    if (lane == 0) {
+    if (gt == 0) {
         mbar_init(&bars[0], 1);
         mbar_init(&bars[1], 1);
         fence_barrier_init();
     }
-    __syncwarp();
+    sync();
     auto issue = [&](long long g, int s) {
-        if (lane == 0) {
+        if (gt == 0) {
             fence_proxy_async_smem();
             mbar_arrive_expect_tx(&bars[s], STAGE_BYTES);
             const long long m = g / NG, gl = g % NG;
@@ -526,8 +547,8 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         }
     };
 
-    const long long nw = (long long)gridDim.x * ZLINE_WARPS;
-    long long g = (long long)blockIdx.x * ZLINE_WARPS + warp;
+    const long long nw = (long long)gridDim.x * NGRP;
+    long long g = (long long)blockIdx.x * NGRP + grp;
     const long long NGT = NG * nmem;   // work items over all members
     uint32_t phase = 0;                // bit s = parity to wait for on stage s
     T um = T(0);
@@ -545,12 +566,20 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
     for (; g < NGT; g += nw, s ^= 1) {
         const bool more = g + nw < NGT;
         if (more) issue(g + nw, s ^ 1);
-        const bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], (phase >> s) & 1u));
+        // every thread waits (bounded) for the copies; the group agrees on the outcome
+        bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], (phase >> s) & 1u));
+        if constexpr (GW > 1) {
+            if (lane == 0) votes[gt >> 5] = ok ? 1 : 0;
+            sync();
+#pragma unroll
+            for (int w = 0; w < GW; ++w) ok = ok && votes[w] != 0;
+            sync();   // votes read before they are written again
+        }
         phase ^= 1u << s;
         if (!ok) {
             // record the timeout, let the copy already issued for the next group land, leave
             if (more) (void)mbar_wait(&bars[s ^ 1], (phase >> (s ^ 1)) & 1u);
-            if (lane == 0) atomicExch(&sd[g / NG].status, kStatusTimeout);
+            if (gt == 0) atomicExch(&sd[g / NG].status, kStatusTimeout);
             return;
         }
         const long long mem = g / NG;
@@ -588,7 +617,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         load_pair(0, V1);
         load_pair(2, V2);
         load_pair(4, V3);
-        __syncwarp();   // every lane has read the staged lines before the buffer is reused
+        sync();   // every lane has read the staged lines before the buffer is reused
         PL::inv(V1, sb, p, tw, sidx, sync);
         PL::inv(V2, sb, p, tw, sidx, sync);
         PL::inv(V3, sb, p, tw, sidx, sync);
@@ -604,7 +633,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         PL::fwd(V1, sb, p, tw, sidx, sync);
 #pragma unroll
         for (int q = 0; q < E; ++q) sb[sidx(p + P * q)] = V1[q];
-        __syncwarp();
+        sync();
         {
             cx<T>* outA = Wm + line * NZP;
             cx<T>* outB = outA + G::FS;
@@ -621,7 +650,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
                 }
             }
         }
-        __syncwarp();
+        sync();
         // Nz (real input): its spectrum is the transform itself
         PL::fwd(V2, sb, p, tw, sidx, sync);
         cx<T>* outC = Wm + 2 * G::FS + line * NZP;
@@ -633,7 +662,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         // the stage buffer is refilled by a bulk copy (async proxy) next iteration:
         // order every lane's exchange accesses to it before that
         fence_proxy_async_smem();
-        __syncwarp();
+        sync();
     }
     flush_umax();
 }

@@ -66,3 +66,26 @@ def test_fp64_has_one_shape(ns3d):
     best, tried = ns3d.autotune(32, steps=3, precision="fp64", nu=0.01, dt=1e-3)
     assert len(tried) == 1 and best["zform"] == 1
     ns3d.tuning_clear()
+
+
+def test_line_kernel_1024_matches_cta_pass(ns3d):
+    """1024-point z lines span two warps (named-barrier exchanges): the persistent
+    line kernel and the CTA-synchronous pass give the same step to FP32 rounding
+    (compared through the spectra; the state itself is 26 GB on the host)."""
+    N = 1024
+    res = []
+    for z in (0, 1):
+        ns3d.tuning_set(N, 0, z)
+        s = ns3d.Solver(N, nu=4e-4, dt=5e-4, precision="fp32", forcing="SHELL", force_k=2)
+        s.InitialConditions("SPECTRUM", seed=1, k0=4.0)
+        s.RK4Step(2)
+        tot, Ek, Ok = s.ComputeSystemMeasurables()
+        res.append((tot, Ek, Ok))
+        s.close()
+    ns3d.tuning_clear()
+    (t0, E0, O0), (t1, E1, O1) = res
+    for key in ("energy", "enstrophy", "dissipation"):
+        assert abs(t0[key] / t1[key] - 1) < 1e-6, key
+    # FP32 round-off is relative to the spectrum's peak (its tail sits ~20 decades down)
+    assert np.max(np.abs(E0 - E1)) < 1e-6 * E1.max()
+    assert np.max(np.abs(O0 - O1)) < 1e-6 * O1.max()
