@@ -73,17 +73,23 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 #ifndef NS3D_TILE_X32
 #define NS3D_TILE_X32 16
 #endif
+// MINB / MINB_XI: CTAs per SM the x-forward / x-inverse passes are compiled
+// for (registers capped to fit)
 template <int V> struct TileVar;
-template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32; };
-template <> struct TileVar<1> { static constexpr int A = 4, X = 8; };
-template <> struct TileVar<2> { static constexpr int A = 16, X = 8; };
-template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16; };
-template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 8; };
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; };
+template <> struct TileVar<1> { static constexpr int A = 4, X = 8, MINB = 1, MINB_XI = 1; };
+template <> struct TileVar<2> { static constexpr int A = 16, X = 8, MINB = 1, MINB_XI = 1; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16, MINB = 1, MINB_XI = 1; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; };
+template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; };
 
-// Plans of variant V: variants 3 and 4 give the x passes a plan with twice
-// the elements per thread (half the threads per pencil), with 16 pencils per
-// CTA (every row access a full 128-byte segment) or 8 (more registers per
-// thread at the largest sizes).
+// Variant 5: the default tiles and plans with the x-forward pass compiled for
+// two CTAs per SM, so one CTA's FFT overlaps another's loads (the x-inverse
+// pass spills too much at 64 registers to gain from the same).
+// Variant 4: 4-pencil x tiles (half-size CTAs, twice as many per SM).
+// Plans of variant V: variant 3 gives the x passes a plan with twice the
+// elements per thread (half the threads per pencil), with 16 pencils per CTA
+// (every row access a full 128-byte segment).
 template <int N> struct AltX { using X = typename Plans<N>::X; };
 template <> struct AltX<64> { using X = Plan<64, 16, 16, 4>; };
 template <> struct AltX<128> { using X = Plan<128, 16, 16, 8>; };
@@ -91,7 +97,7 @@ template <> struct AltX<256> { using X = Plan<256, 16, 16, 16>; };
 template <> struct AltX<512> { using X = Plan<512, 16, 8, 8, 8>; };
 template <int N, int V> struct PlansV {
     using A = typename Plans<N>::A;
-    using X = typename std::conditional<(V >= 3), typename AltX<N>::X, typename Plans<N>::X>::type;
+    using X = typename std::conditional<(V == 3), typename AltX<N>::X, typename Plans<N>::X>::type;
 };
 template <int P, int W> constexpr int clip_tile() { return P * W <= 512 ? W : (P * 8 <= 512 ? 8 : (P * 4 <= 512 ? 4 : 2)); }
 template <typename T, int N, int V = 0> constexpr int tile_a() {
@@ -168,7 +174,7 @@ enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAI
 // registers, so the five transforms below read each input once.
 // ---------------------------------------------------------------------------
 template <typename T, int N, int V = 0>
-__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P)
+__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, TileVar<V>::MINB_XI)
 k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
     using PL = typename PlansV<N, V>::X;
@@ -675,7 +681,7 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
 // error partial sums go to dpart[member][block][3] in a fixed order.
 // ---------------------------------------------------------------------------
 template <typename T, int N, int INTEG, int MODE, int V = 0>
-__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P)
+__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, TileVar<V>::MINB)
 k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
        cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
        const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs, cx<T>* __restrict__ K,

@@ -224,7 +224,7 @@ def run_ours(args, ws, rank, local):
     tuned = None
     if not args.no_autotune:
         # the library's autotuner picks the tile / radix variant and z-pass form of this size (untimed)
-        tuned, _ = pkg.autotune(N, steps=10, **cfg)
+        tuned, _ = pkg.autotune(N, steps=20, **cfg)
     s = pkg.Solver(N, **cfg)
     s.InitialConditions("SPECTRUM", seed=0, k0=4.0, energy=1.0)
     stream = torch.cuda.ExternalStream(s.stream)
