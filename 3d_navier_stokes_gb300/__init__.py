@@ -48,7 +48,7 @@ EXPORTS = (
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
     "ns3d_les_infer_host", "ns3d_les_profile_infer", "ns3d_io_bytes",
     "ns3d_autotune", "ns3d_autotune_ensemble", "ns3d_tuning_get", "ns3d_tuning_set", "ns3d_tuning_clear", "ns3d_tuning_save",
-    "ns3d_tuning_load",
+    "ns3d_tuning_load", "ns3d_increment_stats",
 )
 
 
@@ -173,6 +173,8 @@ def lib():
         L.ns3d_tuning_save.argtypes = [ctypes.c_char_p]
         L.ns3d_tuning_load.restype = I
         L.ns3d_tuning_load.argtypes = [ctypes.c_char_p]
+        L.ns3d_increment_stats.restype = I
+        L.ns3d_increment_stats.argtypes = [P, ctypes.POINTER(ctypes.c_int), I, I, D, D, D]
         L.ns3d_io_bytes.restype = I
         L.ns3d_io_bytes.argtypes = [P, ctypes.POINTER(ctypes.c_longlong), ctypes.POINTER(ctypes.c_longlong)]
         L.ns3d_stream.restype = P
@@ -457,6 +459,18 @@ class Solver:
         v = ctypes.c_double()
         self._ck(lib().ns3d_max_speed_sum(self._h, ctypes.byref(v)))
         return v.value
+
+    def increment_stats(self, increments=None, n_bins: int = 1000):
+        """Longitudinal velocity-increment statistics (min, max, mean, sd, skew, excess
+        kurtosis per increment), bin edges and counts; increments None: 1, 2, ..., 128, N/2."""
+        inc = None if increments is None else np.ascontiguousarray(increments, dtype=np.int32)
+        nr = 9 if inc is None else len(inc)
+        stats = np.zeros((nr, 6))
+        ranges = np.zeros((nr, n_bins + 1))
+        counts = np.zeros((nr, n_bins))
+        ip = None if inc is None else inc.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        self._ck(lib().ns3d_increment_stats(self._h, ip, nr, n_bins, _dp(stats), _dp(ranges), _dp(counts)))
+        return {"stats": stats, "ranges": ranges, "counts": counts}
 
     def io_bytes(self):
         """(host->device, device->host) bytes moved over the host link by the last upload / download."""

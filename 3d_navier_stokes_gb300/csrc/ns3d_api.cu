@@ -261,6 +261,21 @@ ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* c, double atol, double rtol) {
     return pass(c, c->impl->set_dp_tolerances(atol, rtol));
 }
 
+ns3d_status ns3d_increment_stats(ns3d_ctx* c, const int* increments, int n_incr, int n_bins, double* stats,
+                                 double* ranges, double* counts) {
+    if (!c || !stats || n_bins < 1 || n_bins > 12288) return NS3D_ERR_INVALID;
+    const int N = c->p.N;
+    const int deflt[9] = {1, 2, 4, 8, 16, 32, 64, 128, N / 2};   // stats.c:411-413
+    if (!increments) {
+        increments = deflt;
+        n_incr = 9;
+    }
+    if (n_incr < 1) return NS3D_ERR_INVALID;
+    for (int r = 0; r < n_incr; ++r)
+        if (increments[r] < 1) return NS3D_ERR_INVALID;
+    return pass(c, c->impl->increment_stats(increments, n_incr, n_bins, stats, ranges, counts));
+}
+
 ns3d_status ns3d_io_bytes(ns3d_ctx* c, long long* h2d, long long* d2h) {
     if (!c) return NS3D_ERR_INVALID;
     return pass(c, c->impl->io_bytes(h2d, d2h));

@@ -46,6 +46,8 @@ class Base {
     virtual ns3d_status set_dp_tolerances(double atol, double rtol) = 0;
     virtual ns3d_status dp_stats(double* err, long* rejects) = 0;
     virtual ns3d_status io_bytes(long long* h2d, long long* d2h) = 0;
+    virtual ns3d_status increment_stats(const int* incr, int nr, int nbins, double* stats, double* ranges,
+                                        double* counts) = 0;
     virtual void* state_ptr() = 0;
     // ensembles: number of members, selection of the member that single-run
     // calls act on, enqueueing one step of every member on the engine's

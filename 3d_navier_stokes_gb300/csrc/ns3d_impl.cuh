@@ -805,6 +805,69 @@ class Impl final : public Base {
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;
     }
+    // longitudinal velocity-increment statistics of the current state (stats.cuh)
+    ns3d_status increment_stats(const int* incr, int nr, int nbins, double* stats, double* ranges,
+                                double* counts) override {
+        ns3d_status st = ensure_real();
+        if (st != NS3D_OK) return st;
+        p1(U_, m_, 1); p2(m_, 1);
+        k_zpass<T, N, 1><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
+            Wm(m_), tw_, real_, nullptr, 0);
+        double *part = nullptr, *red = nullptr;
+        unsigned long long* cnt = nullptr;
+        cudaError_t e = cudaMalloc(&part, sizeof(double) * (kIncrParts * 4 + 8));
+        if (e == cudaSuccess) e = cudaMalloc(&cnt, sizeof(unsigned long long) * nbins);
+        red = part + kIncrParts * 4;   // [0..3] reduced values, [4] mean, [5..6] lo, hi
+        std::vector<unsigned long long> hc(nbins);
+        double h[8];
+        for (int r = 0; r < nr && e == cudaSuccess; ++r) {
+            const int dr = incr[r];
+            k_incr_moments<T, N><<<kIncrParts, kIncrThreads, 0, s_>>>(real_, dr, 0, nullptr, part);
+            k_incr_reduce<><<<1, 32, 0, s_>>>(part, kIncrParts, 0, red);
+            e = cudaMemcpyAsync(h, red, sizeof(double) * 4, cudaMemcpyDeviceToHost, s_);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+            if (e != cudaSuccess) break;
+            const double n = h[0], mn = n > 0 ? h[2] : 0.0, mx = n > 0 ? h[3] : 0.0, mean = n > 0 ? h[1] / n : 0.0;
+            double m2 = 0, m3 = 0, m4 = 0;
+            const double lo = mn - 0.05, hi = mx + 0.05;
+            for (int b = 0; b < nbins; ++b) hc[b] = 0;
+            if (n > 0) {
+                const double lh[3] = {mean, lo, hi};
+                e = cudaMemcpyAsync(red + 4, lh, sizeof(double) * 3, cudaMemcpyHostToDevice, s_);
+                if (e != cudaSuccess) break;
+                k_incr_moments<T, N><<<kIncrParts, kIncrThreads, 0, s_>>>(real_, dr, 1, red + 4, part);
+                k_incr_reduce<><<<1, 32, 0, s_>>>(part, kIncrParts, 1, red);
+                e = cudaMemsetAsync(cnt, 0, sizeof(unsigned long long) * nbins, s_);
+                if (e != cudaSuccess) break;
+                k_incr_hist<T, N><<<kIncrParts, kIncrThreads, sizeof(unsigned) * nbins, s_>>>(real_, dr, red + 5, nbins,
+                                                                                              cnt);
+                e = cudaMemcpyAsync(h, red, sizeof(double) * 4, cudaMemcpyDeviceToHost, s_);
+                if (e == cudaSuccess) e = cudaMemcpyAsync(hc.data(), cnt, sizeof(unsigned long long) * nbins,
+                                                          cudaMemcpyDeviceToHost, s_);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(s_);
+                if (e != cudaSuccess) break;
+                m2 = h[0]; m3 = h[1]; m4 = h[2];
+            }
+            // GSL rstat definitions: sample sd (n - 1), skew = m3 / sd^3, excess kurtosis m4 / sd^4 - 3
+            const double var = n > 1 ? m2 / (n - 1) : 0.0;
+            double* sr = stats + 6 * r;
+            sr[0] = mn; sr[1] = mx; sr[2] = mean; sr[3] = sqrt(var);
+            sr[4] = var > 0 ? (m3 / n) / pow(var, 1.5) : 0.0;
+            sr[5] = var > 0 ? (m4 / n) / (var * var) - 3.0 : 0.0;
+            if (ranges)
+                for (int b = 0; b <= nbins; ++b) ranges[(long long)r * (nbins + 1) + b] = incr_edge(lo, hi, b, nbins);
+            if (counts)
+                for (int b = 0; b < nbins; ++b) counts[(long long)r * nbins + b] = (double)hc[b];
+        }
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (part) cudaFree(part);
+        if (cnt) cudaFree(cnt);
+        if (e != cudaSuccess) {
+            set_err("increment statistics: %s", cudaGetErrorString(e));
+            return NS3D_ERR_CUDA;
+        }
+        return NS3D_OK;
+    }
     ns3d_status io_bytes(long long* h2d, long long* d2h) override {
         if (h2d) *h2d = io_h2d_;
         if (d2h) *d2h = io_d2h_;

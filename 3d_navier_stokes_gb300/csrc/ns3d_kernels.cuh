@@ -28,6 +28,7 @@
 #include <type_traits>
 
 #include "fft_engine.cuh"
+#include "stats.cuh"
 #include "tma.cuh"
 
 namespace ns3d {

@@ -155,6 +155,18 @@ ns3d_status ns3d_set_forcing_target(ns3d_ctx* ctx, double e);
 ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* ctx, double atol, double rtol);
 ns3d_status ns3d_dp_stats(ns3d_ctx* ctx, double* last_err, long* rejects);
 
+/* Longitudinal velocity-increment statistics of the current state, the
+ * post-processing of PostProcessing/src/stats.c:22-254 on the GPU. For each
+ * increment r (grid points) the samples u_a(x + r e_a) - u_a(x) for a = x, y, z
+ * with x_a + r < N (not periodic) are pooled; stats[r][6] = min, max, mean,
+ * sample sd, skewness m3/sd^3 and excess kurtosis m4/sd^4 - 3 (GSL rstat);
+ * ranges[r][n_bins + 1] = n_bins uniform bins over [min - 0.05, max + 0.05]
+ * (GSL's uniform edges); counts[r][n_bins] with edge[b] <= d < edge[b + 1].
+ * increments NULL: {1, 2, 4, 8, 16, 32, 64, 128, N/2} (n_incr = 9, the
+ * reference's NUM_INCR); ranges / counts may be NULL. n_bins <= 12288. */
+ns3d_status ns3d_increment_stats(ns3d_ctx* ctx, const int* increments, int n_incr, int n_bins, double* stats,
+                                 double* ranges, double* counts);
+
 /* Largest |u|+|v|+|w| over the grid for the current state (CFL numerator). */
 ns3d_status ns3d_max_speed_sum(ns3d_ctx* ctx, double* umax);
 

@@ -934,3 +934,93 @@ void orc_real_space(orc_ctx* c, double* u, double* w) {
         for (long n = 0; n < 3 * c->nR; ++n) w[n] *= s;
     }
 }
+
+/* ------------------------------------------------------------------------ */
+/* Longitudinal velocity-increment statistics, restating the post-processing */
+/* PostProcessing/src/stats.c:22-254 (Precompute, ComputeStats) and          */
+/* AllocateStatsObjects (:404-418): for each increment r the samples         */
+/* u_a(x + r e_a) - u_a(x), a = x, y, z, with x_a + r < N, pooled. GSL's      */
+/* running statistics give min, max, mean, sample sd, skewness m3/sd^3 and    */
+/* excess kurtosis m4/sd^4 - 3; here they come from two passes with long      */
+/* double sums. Bins: gsl_histogram_set_ranges_uniform over                  */
+/* [min - 0.05, max + 0.05], edge b = ((n-b)/n) lo + (b/n) hi, sample d in   */
+/* bin b when edge[b] <= d < edge[b+1] (binary search).                      */
+/* ------------------------------------------------------------------------ */
+static double incr_edge(double lo, double hi, int b, int n) {
+    return ((double)(n - b) / (double)n) * lo + ((double)b / (double)n) * hi;
+}
+
+void orc_increment_stats(orc_ctx* c, const int* incr, int nr, int nbins, double* stats, double* ranges,
+                         double* counts) {
+    const int N = c->N;
+    const long NP = N + 2;
+    double* u = (double*)malloc(sizeof(double) * 3 * (size_t)c->nR);
+    orc_real_space(c, u, NULL);
+    /* u[((i*N + j)*(N+2) + k)*3 + a] */
+#define UAT(i, j, k, a) u[(((long)(i) * N + (j)) * NP + (k)) * 3 + (a)]
+    double* edges = (double*)malloc(sizeof(double) * (nbins + 1));
+    for (int r = 0; r < nr; ++r) {
+        const int dr = incr[r];
+        long double n = 0, s1 = 0;
+        double mn = 0, mx = 0;
+        int first = 1;
+        for (int pass = 0; pass < 3; ++pass) {
+            long double m2 = 0, m3 = 0, m4 = 0;
+            const double mean = n > 0 ? (double)(s1 / n) : 0.0;
+            const double lo = mn - 0.05, hi = mx + 0.05;
+            if (pass == 2)
+                for (int b = 0; b <= nbins; ++b) edges[b] = incr_edge(lo, hi, b, nbins);
+            if (pass == 2 && counts)
+                for (int b = 0; b < nbins; ++b) counts[(long)r * nbins + b] = 0.0;
+            for (int i = 0; i < N; ++i)
+                for (int j = 0; j < N; ++j)
+                    for (int k = 0; k < N; ++k) {
+                        for (int a = 0; a < 3; ++a) {
+                            const int ca = a == 0 ? i : a == 1 ? j : k;
+                            if (ca + dr >= N) continue;
+                            const double d = (a == 0 ? UAT(i + dr, j, k, 0) : a == 1 ? UAT(i, j + dr, k, 1)
+                                                                                      : UAT(i, j, k + dr, 2)) -
+                                             UAT(i, j, k, a);
+                            if (pass == 0) {
+                                n += 1;
+                                s1 += d;
+                                if (first || d < mn) mn = d;
+                                if (first || d > mx) mx = d;
+                                first = 0;
+                            } else if (pass == 1) {
+                                const long double e = (long double)d - mean;
+                                m2 += e * e;
+                                m3 += e * e * e;
+                                m4 += e * e * e * e;
+                            } else if (counts) {
+                                /* binary search for edge[b] <= d < edge[b+1] */
+                                int lo_b = 0, hi_b = nbins;
+                                while (hi_b - lo_b > 1) {
+                                    const int mid = (lo_b + hi_b) / 2;
+                                    if (d >= edges[mid]) lo_b = mid;
+                                    else hi_b = mid;
+                                }
+                                counts[(long)r * nbins + lo_b] += 1.0;
+                            }
+                        }
+                    }
+            if (pass == 1) {
+                const double nn = (double)n;
+                const double var = nn > 1 ? (double)(m2 / (n - 1)) : 0.0;
+                double* sr = stats + 6 * r;
+                sr[0] = n > 0 ? mn : 0.0;
+                sr[1] = n > 0 ? mx : 0.0;
+                sr[2] = mean;
+                sr[3] = sqrt(var);
+                sr[4] = var > 0 ? (double)(m3 / n) / pow(var, 1.5) : 0.0;
+                sr[5] = var > 0 ? (double)(m4 / n) / (var * var) - 3.0 : 0.0;
+                if (n == 0) mn = mx = 0.0;
+            }
+        }
+        if (ranges)
+            for (int b = 0; b <= nbins; ++b) ranges[(long)r * (nbins + 1) + b] = edges[b];
+    }
+#undef UAT
+    free(edges);
+    free(u);
+}

@@ -68,6 +68,11 @@ void orc_measurables(orc_ctx* c, double* totals5, double* Ek, double* Ok);
 int  orc_ic(orc_ctx* c, const char* name, uint64_t seed, double k0, double energy);
 void orc_real_space(orc_ctx* c, double* u, double* w);
 double orc_max_speed_sum(orc_ctx* c);
+/* longitudinal velocity-increment statistics (PostProcessing/src/stats.c):
+   stats[r][6] = min, max, mean, sd, skew, excess kurtosis; ranges[r][nbins+1];
+   counts[r][nbins] */
+void orc_increment_stats(orc_ctx* c, const int* incr, int nr, int nbins, double* stats, double* ranges,
+                         double* counts);
 
 #ifdef __cplusplus
 }

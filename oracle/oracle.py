@@ -79,6 +79,8 @@ def lib():
         L.orc_step.argtypes = [P, ctypes.c_int]
         L.orc_step.restype = ctypes.c_int
         L.orc_dp_stats.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p]
+        L.orc_increment_stats.argtypes = [P, ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p]
         L.orc_measurables.argtypes = [P, D, D, D]
         L.orc_ic.restype = ctypes.c_int
         L.orc_ic.argtypes = [P, ctypes.c_char_p, ctypes.c_uint64, ctypes.c_double, ctypes.c_double]
@@ -189,6 +191,17 @@ class Oracle:
     def step(self, n=1):
         if lib().orc_step(self._c, n) != 0:
             raise RuntimeError("DP5CN step rejected 50 times in a row")
+
+    def increment_stats(self, increments=None, n_bins=1000):
+        """Longitudinal velocity-increment statistics, bin edges and counts
+        (PostProcessing/src/stats.c); increments None: 1, 2, ..., 128, N/2."""
+        inc = np.ascontiguousarray([1, 2, 4, 8, 16, 32, 64, 128, self.N // 2] if increments is None else increments,
+                                   dtype=np.int32)
+        nr = len(inc)
+        stats, ranges, counts = np.zeros((nr, 6)), np.zeros((nr, n_bins + 1)), np.zeros((nr, n_bins))
+        lib().orc_increment_stats(self._c, inc.ctypes.data, nr, n_bins, stats.ctypes.data, ranges.ctypes.data,
+                                  counts.ctypes.data)
+        return {"stats": stats, "ranges": ranges, "counts": counts}
 
     def dp_stats(self):
         """(error norm of the last DP5CN attempt, rejected attempts so far)"""

@@ -245,3 +245,32 @@ def test_dp5_adaptive_control(oracle):
     t = o.get_time()[0]
     # Taylor–Green at early times: E(t) ~ E0 exp(-6 nu t)
     assert abs(o.measurables()[0][0] / (E0 * np.exp(-6 * 0.01 * t)) - 1) < 5e-3
+
+
+def test_increment_stats_vs_numpy(oracle):
+    """The oracle's increment statistics (PostProcessing/src/stats.c) against an
+    independent numpy computation on the same real-space field."""
+    N, nb = 16, 50
+    o = oracle.Oracle(N, nu=0.01)
+    o.ic("SPECTRUM", seed=6, k0=3.0)
+    got = o.increment_stats([1, 3, 8, 16], n_bins=nb)
+    u, _ = o.real_space()
+    u = u[:, :, :N, :]
+    for r, dr in enumerate([1, 3, 8, 16]):
+        d = np.concatenate([(u[dr:, :, :, 0] - u[:-dr, :, :, 0]).ravel() if dr < N else np.zeros(0),
+                            (u[:, dr:, :, 1] - u[:, :-dr, :, 1]).ravel() if dr < N else np.zeros(0),
+                            (u[:, :, dr:, 2] - u[:, :, :-dr, 2]).ravel() if dr < N else np.zeros(0)])
+        st = got["stats"][r]
+        if d.size == 0:
+            assert np.all(st == 0) and np.all(got["counts"][r] == 0)
+            continue
+        n, m = d.size, d.mean()
+        sd = d.std(ddof=1)
+        ref = [d.min(), d.max(), m, sd, np.mean((d - m) ** 3) / sd ** 3, np.mean((d - m) ** 4) / sd ** 4 - 3]
+        assert np.allclose(st, ref, rtol=1e-10, atol=1e-12)
+        lo, hi = d.min() - 0.05, d.max() + 0.05
+        b = np.arange(nb + 1)
+        edges = ((nb - b) / nb) * lo + (b / nb) * hi
+        assert np.array_equal(got["ranges"][r], edges)
+        idx = np.searchsorted(edges, d, side="right") - 1
+        assert np.array_equal(got["counts"][r], np.bincount(idx, minlength=nb)[:nb].astype(float))
