@@ -75,14 +75,15 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 #define NS3D_TILE_X32 16
 #endif
 // MINB / MINB_XI: CTAs per SM the x-forward / x-inverse passes are compiled
-// for (registers capped to fit)
+// for (registers capped to fit); BATCH: the x-forward epilogue issues all of a
+// thread's state loads of a component before their updates (more registers)
 template <int V> struct TileVar;
-template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; };
-template <> struct TileVar<1> { static constexpr int A = 4, X = 8, MINB = 1, MINB_XI = 1; };
-template <> struct TileVar<2> { static constexpr int A = 16, X = 8, MINB = 1, MINB_XI = 1; };
-template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16, MINB = 1, MINB_XI = 1; };
-template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; };
-template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; };
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; };
+template <> struct TileVar<1> { static constexpr int A = 4, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; };
+template <> struct TileVar<2> { static constexpr int A = 16, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; };
+template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false; };
 
 // Variant 5: the default tiles and plans with the x-forward pass compiled for
 // two CTAs per SM, so one CTA's FFT overlaps another's loads (the x-inverse
@@ -736,6 +737,94 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     T h = T(0);
     if (MODE <= X_STAGE4) h = T(sd->dt);
     const int rem = G::KC2 - ky * ky - kz * kz;
+    if constexpr ((INTEG == INT_IFRK4 || INTEG == INT_RK4CN) && MODE <= X_STAGE4 && TileVar<V>::BATCH) {
+        // RK4-family stages: the projection of every mode of this thread first,
+        // then per component all of its state loads before their updates, so
+        // that E loads (per array) are in flight at once
+        unsigned valid = 0u;
+        cx<T> tb[E];
+#pragma unroll
+        for (int s = 0; s < E; ++s) {
+            const int i = p + P * s;
+            const int kx = kof<N>(i);
+            tb[s] = czero<T>();
+            if (kx * kx > rem) continue;
+            valid |= 1u << s;
+            const int k2 = kx * kx + ky * ky + kz * kz;
+            cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
+            if (sgs && sd->sgs_on) {
+                // learned subgrid term -div(tau), single run only (member 0)
+                const long long q = (long long)i * xs + off;
+                n0 = n0 + sgs[q];
+                n1 = n1 + sgs[G::FS + q];
+                n2 = n2 + sgs[2 * G::FS + q];
+            }
+            if (k2 > 0) {
+                const T kinv = T(1) / T(k2);
+                const cx<T> kdn = n0 * T(kx) + n1 * T(ky) + n2 * T(kz);
+                n0 = n0 - kdn * (T(kx) * kinv);
+                n1 = n1 - kdn * (T(ky) * kinv);
+                n2 = n2 - kdn * (T(kz) * kinv);
+            } else {
+                n0 = n1 = n2 = czero<T>();
+            }
+            F[0][s] = n0;
+            F[1][s] = n1;
+            F[2][s] = n2;
+            tb[s] = ldg(&tab[k2]);
+        }
+        constexpr bool kIF = INTEG == INT_IFRK4;
+        constexpr bool needU = !(kIF && MODE == X_STAGE4);
+        constexpr bool needA = kIF ? (MODE != X_STAGE1) : (MODE != X_STAGE1);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            cx<T> u[E], a[E];
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                u[s] = czero<T>();
+                a[s] = czero<T>();
+                if (!((valid >> s) & 1u)) continue;
+                const long long q = c * G::FS + (long long)(p + P * s) * xs + off;
+                if (needU) u[s] = U[q];
+                if (needA) a[s] = ACC[q];
+            }
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                if (!((valid >> s) & 1u)) continue;
+                const long long q = c * G::FS + (long long)(p + P * s) * xs + off;
+                const cx<T> nn = F[c][s];
+                if constexpr (kIF) {
+                    const T Eh = tb[s].x, Ef = tb[s].y;
+                    if (MODE == X_STAGE1) {
+                        UT[q] = (u[s] + nn * (h * T(0.5))) * Eh;
+                        ACC[q] = (u[s] + nn * (h / T(6))) * Ef;
+                    } else if (MODE == X_STAGE2) {
+                        UT[q] = u[s] * Eh + nn * (h * T(0.5));
+                        ACC[q] = a[s] + nn * (h / T(3) * Eh);
+                    } else if (MODE == X_STAGE3) {
+                        UT[q] = u[s] * Ef + nn * (h * Eh);
+                        ACC[q] = a[s] + nn * (h / T(3) * Eh);
+                    } else {
+                        U[q] = a[s] + nn * (h / T(6));
+                    }
+                } else {
+                    if (MODE == X_STAGE1) {
+                        UT[q] = u[s] + nn * (h * T(0.5));
+                        ACC[q] = nn * (T(1) / T(6));
+                    } else if (MODE == X_STAGE2) {
+                        UT[q] = u[s] + nn * (h * T(0.5));
+                        ACC[q] = a[s] + nn * (T(1) / T(3));
+                    } else if (MODE == X_STAGE3) {
+                        UT[q] = u[s] + nn * h;
+                        ACC[q] = a[s] + nn * (T(1) / T(3));
+                    } else {
+                        U[q] = u[s] * tb[s].x + (a[s] + nn * (T(1) / T(6))) * tb[s].y;
+                    }
+                }
+            }
+        }
+        return;
+    }
     double es[3] = {0.0, 0.0, 0.0};   // DP5CN error partial sums
 #pragma unroll
     for (int s = 0; s < E; ++s) {

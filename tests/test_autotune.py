@@ -16,20 +16,21 @@ def run(ns3d, N, steps=5):
 
 @pytest.mark.parametrize("N", [48, 64, 128])
 def test_tile_variants_are_bit_identical(ns3d, N):
-    """Variants 1, 2, 4 and 5 change only the pencils or CTAs per SM: bit-identical. Variant 3
-    (another x-pass radix plan, where compiled) and the z-pass forms change the
-    order of the butterflies: FP32 rounding."""
+    """Variants 1, 2 and 4 change only the pencils per CTA: bit-identical. Variant 3
+    (another x-pass radix plan, where compiled), variant 5 (the per-mode x-forward
+    epilogue at two CTAs per SM) and the z-pass forms change the order of
+    operations: FP32 rounding."""
     states = {}
     for v in range(6):
         for z in (0, 1):
             ns3d.tuning_set(N, v, z)
             states[(v, z)] = run(ns3d, N)
     ns3d.tuning_clear()
-    for v in (1, 2, 4, 5):
+    for v in (1, 2, 4):
         assert np.array_equal(states[(v, 0)], states[(0, 0)])
         assert np.array_equal(states[(v, 1)], states[(0, 1)])
     ref = states[(0, 0)]
-    for key in ((0, 1), (3, 0), (3, 1)):
+    for key in ((0, 1), (3, 0), (3, 1), (5, 0), (5, 1)):
         assert np.linalg.norm(states[key] - ref) < 1e-6 * np.linalg.norm(ref), key
 
 
