@@ -56,7 +56,13 @@ static ns3d_ctx* ctx_for(double dt) {
         exit(1);
     }
     ns3d_params want = params_from_sys(dt);
-    if (g_ctx && memcmp(&want, &g_params, sizeof(want)) == 0) return g_ctx;
+    if (g_ctx) {
+        /* the step size is time state, not configuration: an adaptive or
+           Dormand-Prince run changes it every step on the same engine */
+        ns3d_params same = want;
+        same.dt = g_params.dt;
+        if (memcmp(&same, &g_params, sizeof(same)) == 0) return g_ctx;
+    }
     if (g_ctx) ns3d_destroy(g_ctx);
     g_ctx = NULL;
     ns3d_status s = ns3d_create(&want, &g_ctx);

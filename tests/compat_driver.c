@@ -2,9 +2,12 @@
  * A reference-shaped driver: the loop of SpectralSolve (solver.c:50-208)
  * written against include/ns3d_compat.h, i.e. the reference's function names
  * and global structs. Used by tests/test_driver_compat.py.
- *   compat_driver N nu dt nsteps integrator(0|1) out.bin
+ *   compat_driver N nu dt nsteps integrator(0..3) out.bin
+ * Integrators 0 and 1 step with RK4Step, 2 and 3 with RK5DPStep (for 3 the
+ * step size follows the Dormand-Prince control through sys_vars->dt).
  * Writes u_hat after nsteps (complex double [N][N][N/2+1][3]) followed by the
- * energy/enstrophy series recorded after every step.
+ * energy/enstrophy series recorded after every step, then sys_vars->t and
+ * sys_vars->dt (set by RK5DPStep for integrator 3).
  */
 #include <stdio.h>
 #include <stdlib.h>
@@ -45,13 +48,18 @@ int main(int argc, char** argv) {
     InitialConditions(rd.u_hat, NULL, sv.N);
     ComputeSystemMeasurables(0);
     for (int it = 1; it <= steps; ++it) {
-        RK4Step(sv.dt, sv.N, sv.local_Nx, &rk);
+        if (sv.integrator >= 2)
+            RK5DPStep(sv.dt, sv.N, it, sv.local_Nx, &rk);
+        else
+            RK4Step(sv.dt, sv.N, sv.local_Nx, &rk);
         ComputeSystemMeasurables(it);
     }
     FILE* f = fopen(argv[6], "wb");
     fwrite(rd.u_hat, sizeof(ns3d_fftw_complex), N * N * NF * 3, f);
     fwrite(rd.tot_energy, sizeof(double), steps + 1, f);
     fwrite(rd.tot_enstr, sizeof(double), steps + 1, f);
+    const double tdt[2] = {sv.t, sv.dt};
+    fwrite(tdt, sizeof(double), 2, f);
     fclose(f);
     ns3d_compat_free();
     return 0;

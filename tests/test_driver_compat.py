@@ -35,7 +35,7 @@ def test_driver_rejects_bad_arguments(ns3d):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("integrator", [0, 1])
+@pytest.mark.parametrize("integrator", [0, 1, 2, 3])
 def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator):
     exe = tmp_path / "compat_driver"
     libdir = os.path.dirname(ns3d.LIB_PATH)
@@ -49,7 +49,7 @@ def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator)
     nf = N * N * (N // 2 + 1) * 3
     u = raw[:2 * nf].view(np.complex128).reshape(N, N, N // 2 + 1, 3)
     E = raw[2 * nf:2 * nf + n + 1]
-    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=oracle.RK4CN if integrator else oracle.IFRK4)
+    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=[oracle.IFRK4, oracle.RK4CN, oracle.RK5CN, oracle.DP5CN][integrator])
     o.ic("TAYLOR_GREEN")
     ref_E = [o.measurables()[0][0]]
     for _ in range(n):
@@ -58,6 +58,12 @@ def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator)
     ref = o.get_state()
     assert np.linalg.norm(u - ref) / np.linalg.norm(ref) < 1e-12
     assert np.max(np.abs(E - ref_E) / np.array(ref_E)) < 1e-12
+    if integrator == 3:
+        # the Dormand-Prince control hands back the new time and the next step size
+        t_ref, dt_ref, _ = o.get_time()
+        t_out, dt_out = raw[2 * nf + 2 * (n + 1):]
+        assert abs(t_out - t_ref) <= 1e-12 * t_ref and abs(dt_out - dt_ref) <= 1e-10 * dt_ref
+        assert dt_out != dt
 
 
 @pytest.mark.gpu
@@ -89,6 +95,43 @@ def test_driver_outputs_match_oracle(ns3d, oracle, tmp_path):
     assert set(k for k in main if not k.startswith("/Iter")) >= {
         "/kx", "/ky", "/kz", "/x", "/y", "/z", "/Time", "/TotalEnergy", "/TotalEnstrophy",
         "/TotalPalinstrophy", "/TotalHelicity", "/EnergyDissipation"}
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("integ", ["rk5cn", "dp5cn"])
+def test_driver_rk5_integrators_match_oracle(ns3d, oracle, tmp_path, integ):
+    """The solver binary with -I rk5cn (fixed step) and -I dp5cn (the
+    Dormand-Prince loop of solver.c:125-194: step while t + dt <= T, record
+    every step) against the oracle driven the same way."""
+    exe = solver_bin(ns3d)
+    N, nu, dt, T = 32, 0.01, 2e-3, 0.02
+    args = [exe, "-o", str(tmp_path), "-n", str(N), "-n", str(N), "-n", str(N), "-s", "0.0", "-e", str(T),
+            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "1", "-I", integ, "-t", "R5"]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    tag = {"rk5cn": "RK5", "dp5cn": "DP5"}[integ]
+    sub = [d for d in os.listdir(tmp_path) if d.startswith(f"SIM_DATA_NAVIER_{tag}_FULL_N[32,32]")]
+    assert len(sub) == 1, os.listdir(tmp_path)
+    main = read_container(os.path.join(tmp_path, sub[0], "Main_HDF_Data.ns3d"))
+    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=oracle.RK5CN if integ == "rk5cn" else oracle.DP5CN)
+    o.ic("TAYLOR_GREEN")
+    ts, E = [0.0], [o.measurables()[0][0]]
+    while True:
+        t, h, _ = o.get_time()
+        if t + h > T + 1e-12 * T:
+            break
+        o.step(1)
+        ts.append(o.get_time()[0])
+        E.append(o.measurables()[0][0])
+    Ts = main["/Time"][0]
+    assert len(Ts) == len(ts)
+    assert np.allclose(Ts, ts, rtol=1e-12, atol=1e-15)
+    assert np.allclose(main["/TotalEnergy"][0], E, rtol=1e-12)
+    steps = np.diff(Ts)
+    if integ == "rk5cn":
+        assert len(Ts) == 11 and np.allclose(steps, dt, rtol=1e-9)
+    else:
+        assert np.ptp(steps) > 1e-3 * dt   # the control changed the step size
 
 
 @pytest.mark.gpu
