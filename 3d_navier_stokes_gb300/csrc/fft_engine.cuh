@@ -87,9 +87,66 @@ __device__ __forceinline__ cx<T> twc(cx<T> a) {
     }
 }
 
+__device__ __forceinline__ float fmat(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmat(double a, double b, double c) { return fma(a, b, c); }
+
+// lo = e + w o, hi = e - w o for a runtime twiddle w: four FMAs form lo and
+// hi = 2e - lo takes two more (6 instructions instead of a complex product
+// and four additions; the absolute error stays within a rounding of |e| + |o|)
+template <typename T>
+__device__ __forceinline__ void bfly_w(cx<T> e, cx<T> o, cx<T> w, cx<T>& lo, cx<T>& hi) {
+    lo = mk(fmat(o.x, w.x, fmat(-o.y, w.y, e.x)), fmat(o.y, w.x, fmat(o.x, w.y, e.y)));
+    hi = mk(fmat(T(2), e.x, -lo.x), fmat(T(2), e.y, -lo.y));
+}
+
+// lo = e + W_R^K o, hi = e - W_R^K o with W_R = exp(-2 pi i / R): additions
+// only for the trivial angles, two additions and four FMAs for the odd
+// multiples of 45 degrees, four FMAs and the 2e - lo form otherwise.
+template <int R, int K, typename T>
+__device__ __forceinline__ void bfly(cx<T> e, cx<T> o, cx<T>& lo, cx<T>& hi) {
+    constexpr int k = K % R;
+    if constexpr (k == 0) {
+        lo = e + o;
+        hi = e - o;
+    } else if constexpr (4 * k == R) {
+        const cx<T> t = mul_mi(o);
+        lo = e + t;
+        hi = e - t;
+    } else if constexpr (2 * k == R) {
+        lo = e - o;
+        hi = e + o;
+    } else if constexpr (4 * k == 3 * R) {
+        const cx<T> t = mul_i(o);
+        lo = e + t;
+        hi = e - t;
+    } else {
+        constexpr bool tri = (R % 3 == 0);
+        constexpr int idx = tri ? (k * 12 / R) : (k * 16 / R);
+        constexpr double cd = tri ? kC12[idx] : kC16[idx];
+        constexpr double sd = tri ? kS12[idx] : kS16[idx];
+        const T c = T(cd), s = T(sd);
+        // W o = (c o.x + s o.y, c o.y - s o.x)
+        if constexpr (!tri && (8 * k) % R == 0 && cd == sd) {          // 1/8, 5/8 turn: (c u, c v)
+            const T u = o.x + o.y, v = o.y - o.x;
+            lo = mk(fmat(c, u, e.x), fmat(c, v, e.y));
+            hi = mk(fmat(-c, u, e.x), fmat(-c, v, e.y));
+        } else if constexpr (!tri && (8 * k) % R == 0 && cd == -sd) {  // 3/8, 7/8 turn: (-c v, c u)
+            const T u = o.x + o.y, v = o.y - o.x;
+            lo = mk(fmat(-c, v, e.x), fmat(c, u, e.y));
+            hi = mk(fmat(c, v, e.x), fmat(-c, u, e.y));
+        } else {
+            lo = mk(fmat(c, o.x, fmat(s, o.y, e.x)), fmat(c, o.y, fmat(-s, o.x, e.y)));
+            hi = mk(fmat(T(2), e.x, -lo.x), fmat(T(2), e.y, -lo.y));
+        }
+    }
+}
+
 // ---------------------------------------------------------------------------
 // Forward DFT codelets, in place on a[0..R-1] (natural order in and out).
 // Even sizes are split decimation-in-time into two halves.
+//   run(a)        : X = DFT(a)
+//   run_tw<ONE>(a, w): X = DFT(a[r] w[r]), the stage twiddles folded into the
+//                   first butterfly level (w[0] is 1 and unread when ONE)
 // ---------------------------------------------------------------------------
 template <int R, typename T> struct Dft;
 
@@ -102,6 +159,11 @@ template <typename T> struct Dft<2, T> {
         a[0] = t + a[1];
         a[1] = t - a[1];
     }
+    template <bool ONE>
+    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
+        const cx<T> x0 = ONE ? a[0] : cmul(a[0], w[0]);
+        bfly_w(x0, a[1], w[1], a[0], a[1]);
+    }
 };
 template <typename T> struct Dft<3, T> {
     __device__ __forceinline__ static void run(cx<T>* a) {
@@ -113,24 +175,40 @@ template <typename T> struct Dft<3, T> {
         a[1] = m + jd;
         a[2] = m - jd;
     }
+    template <bool ONE>
+    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
+        if (!ONE) a[0] = cmul(a[0], w[0]);
+        a[1] = cmul(a[1], w[1]);
+        a[2] = cmul(a[2], w[2]);
+        run(a);
+    }
 };
 template <typename T> struct Dft<4, T> {
-    __device__ __forceinline__ static void run(cx<T>* a) {
-        cx<T> s02 = a[0] + a[2], d02 = a[0] - a[2];
-        cx<T> s13 = a[1] + a[3], d13 = mul_mi(a[1] - a[3]);
+    __device__ __forceinline__ static void finish(cx<T>* a, cx<T> s02, cx<T> d02, cx<T> s13, cx<T> d13) {
+        d13 = mul_mi(d13);
         a[0] = s02 + s13;
         a[2] = s02 - s13;
         a[1] = d02 + d13;
         a[3] = d02 - d13;
+    }
+    __device__ __forceinline__ static void run(cx<T>* a) {
+        finish(a, a[0] + a[2], a[0] - a[2], a[1] + a[3], a[1] - a[3]);
+    }
+    template <bool ONE>
+    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
+        const cx<T> x0 = ONE ? a[0] : cmul(a[0], w[0]);
+        const cx<T> x1 = cmul(a[1], w[1]);
+        cx<T> s02, d02, s13, d13;
+        bfly_w(x0, a[2], w[2], s02, d02);
+        bfly_w(x1, a[3], w[3], s13, d13);
+        finish(a, s02, d02, s13, d13);
     }
 };
 
 template <int R, typename T, int K = 0>
 __device__ __forceinline__ void combine_half(cx<T>* e, cx<T>* o, cx<T>* a) {
     if constexpr (K < R / 2) {
-        cx<T> t = twc<R, K>(o[K]);
-        a[K] = e[K] + t;
-        a[K + R / 2] = e[K] - t;
+        bfly<R, K>(e[K], o[K], a[K], a[K + R / 2]);
         combine_half<R, T, K + 1>(e, o, a);
     }
 }
@@ -146,6 +224,20 @@ template <int R, typename T> struct Dft {
         }
         Dft<R / 2, T>::run(e);
         Dft<R / 2, T>::run(o);
+        combine_half<R, T>(e, o, a);
+    }
+    template <bool ONE>
+    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
+        cx<T> e[R / 2], o[R / 2], we[R / 2], wo[R / 2];
+#pragma unroll
+        for (int i = 0; i < R / 2; ++i) {
+            e[i] = a[2 * i];
+            o[i] = a[2 * i + 1];
+            we[i] = w[2 * i];
+            wo[i] = w[2 * i + 1];
+        }
+        Dft<R / 2, T>::template run_tw<ONE>(e, we);
+        Dft<R / 2, T>::template run_tw<false>(o, wo);
         combine_half<R, T>(e, o, a);
     }
 };
@@ -175,10 +267,14 @@ __device__ __forceinline__ void fft_stages(cx<T> (&v)[E], cx<T>* sbuf, int p,
         if constexpr (Ns > 1) {
             jm = j % Ns;
             constexpr int step = N / (Ns * R);
+            cx<T> w[R];
+            w[0] = mk(T(1), T(0));
 #pragma unroll
-            for (int r = 1; r < R; ++r) a[r] = cmul(a[r], ldg(&tw[r * jm * step]));
+            for (int r = 1; r < R; ++r) w[r] = ldg(&tw[r * jm * step]);
+            Dft<R, T>::template run_tw<true>(a, w);
+        } else {
+            Dft<R, T>::run(a);
         }
-        Dft<R, T>::run(a);
         if constexpr (last) {
 #pragma unroll
             for (int r = 0; r < R; ++r) v[q + r * Q] = a[r];

@@ -255,7 +255,8 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // Forward: inputs every y, outputs only where ky^2 + kz^2 <= KC^2.
 // ---------------------------------------------------------------------------
 template <typename T, int N, bool INV, int V = 0>
-__global__ void __launch_bounds__(tile_a<T, N, V>() * Plans<N>::A::P)
+__global__ void __launch_bounds__(tile_a<T, N, V>() * Plans<N>::A::P,
+                                  (1024 / (tile_a<T, N, V>() * Plans<N>::A::P) > 0 ? 1024 / (tile_a<T, N, V>() * Plans<N>::A::P) : 1))
 k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
