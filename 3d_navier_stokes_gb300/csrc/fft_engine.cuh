@@ -65,28 +65,6 @@ __device__ constexpr double kS12[12] = {
     0.0, 0.5, 0.86602540378443864676, 1.0, 0.86602540378443864676, 0.5,
     0.0, -0.5, -0.86602540378443864676, -1.0, -0.86602540378443864676, -0.5};
 
-// a * W_R^K with W_R = exp(-2 pi i / R); exact for the trivial angles.
-template <int R, int K, typename T>
-__device__ __forceinline__ cx<T> twc(cx<T> a) {
-    constexpr int k = K % R;
-    if constexpr (k == 0) {
-        return a;
-    } else if constexpr (4 * k == R) {
-        return mul_mi(a);
-    } else if constexpr (2 * k == R) {
-        return mk(-a.x, -a.y);
-    } else if constexpr (4 * k == 3 * R) {
-        return mul_i(a);
-    } else {
-        constexpr bool tri = (R % 3 == 0);
-        constexpr int idx = tri ? (k * 12 / R) : (k * 16 / R);
-        const T c = T(tri ? kC12[idx] : kC16[idx]);
-        const T s = T(tri ? kS12[idx] : kS16[idx]);
-        // (a.x + i a.y)(c - i s)
-        return mk(a.x * c + a.y * s, a.y * c - a.x * s);
-    }
-}
-
 __device__ __forceinline__ float fmat(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return fma(a, b, c); }
 
@@ -148,87 +126,90 @@ __device__ __forceinline__ void bfly(cx<T> e, cx<T> o, cx<T>& lo, cx<T>& hi) {
 //   run_tw<ONE>(a, w): X = DFT(a[r] w[r]), the stage twiddles folded into the
 //                   first butterfly level (w[0] is 1 and unread when ONE)
 // ---------------------------------------------------------------------------
-template <int R, typename T> struct Dft;
+template <int R, typename C> struct Dft;   // C = cx<T>
 
-template <typename T> struct Dft<1, T> {
-    __device__ __forceinline__ static void run(cx<T>*) {}
+template <typename C> struct Dft<1, C> {
+    __device__ __forceinline__ static void run(C*) {}
 };
-template <typename T> struct Dft<2, T> {
-    __device__ __forceinline__ static void run(cx<T>* a) {
-        cx<T> t = a[0];
-        a[0] = t + a[1];
-        a[1] = t - a[1];
-    }
-    template <bool ONE>
-    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
-        const cx<T> x0 = ONE ? a[0] : cmul(a[0], w[0]);
+template <typename C> struct Dft<2, C> {
+    __device__ __forceinline__ static void run(C* a) { bfly<2, 0>(a[0], a[1], a[0], a[1]); }
+    template <bool ONE, typename Wt>
+    __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
+        const C x0 = ONE ? a[0] : cmul(a[0], w[0]);
         bfly_w(x0, a[1], w[1], a[0], a[1]);
     }
 };
-template <typename T> struct Dft<3, T> {
-    __device__ __forceinline__ static void run(cx<T>* a) {
+// scalar type of an element, and -i h d for a real h
+template <typename C> struct RealOf;
+template <typename T> struct RealOf<cx<T>> { using type = T; };
+template <typename T> __device__ __forceinline__ cx<T> mi_scale(cx<T> d, T h) { return mk(d.y * h, -d.x * h); }
+
+template <typename C> struct Dft<3, C> {
+    using T = typename RealOf<C>::type;
+    __device__ __forceinline__ static void run(C* a) {
         const T h = T(0.86602540378443864676);
-        cx<T> s = a[1] + a[2], d = a[1] - a[2];
-        cx<T> m = a[0] - s * T(0.5);
+        C s = a[1] + a[2], d = a[1] - a[2];
+        C m = a[0] - s * T(0.5);
         a[0] = a[0] + s;
-        cx<T> jd = mk(d.y * h, -d.x * h);   // -i*sin(60)*d
+        C jd = mi_scale(d, h);   // -i*sin(60)*d
         a[1] = m + jd;
         a[2] = m - jd;
     }
-    template <bool ONE>
-    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
+    template <bool ONE, typename Wt>
+    __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
         if (!ONE) a[0] = cmul(a[0], w[0]);
         a[1] = cmul(a[1], w[1]);
         a[2] = cmul(a[2], w[2]);
         run(a);
     }
 };
-template <typename T> struct Dft<4, T> {
-    __device__ __forceinline__ static void finish(cx<T>* a, cx<T> s02, cx<T> d02, cx<T> s13, cx<T> d13) {
-        d13 = mul_mi(d13);
-        a[0] = s02 + s13;
-        a[2] = s02 - s13;
-        a[1] = d02 + d13;
-        a[3] = d02 - d13;
+template <typename C> struct Dft<4, C> {
+    __device__ __forceinline__ static void finish(C* a, C s02, C d02, C s13, C d13) {
+        bfly<4, 0>(s02, s13, a[0], a[2]);
+        bfly<4, 1>(d02, d13, a[1], a[3]);   // d02 -/+ i d13
     }
-    __device__ __forceinline__ static void run(cx<T>* a) {
-        finish(a, a[0] + a[2], a[0] - a[2], a[1] + a[3], a[1] - a[3]);
+    __device__ __forceinline__ static void run(C* a) {
+        C s02, d02, s13, d13;
+        bfly<2, 0>(a[0], a[2], s02, d02);
+        bfly<2, 0>(a[1], a[3], s13, d13);
+        finish(a, s02, d02, s13, d13);
     }
-    template <bool ONE>
-    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
-        const cx<T> x0 = ONE ? a[0] : cmul(a[0], w[0]);
-        const cx<T> x1 = cmul(a[1], w[1]);
-        cx<T> s02, d02, s13, d13;
+    template <bool ONE, typename Wt>
+    __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
+        const C x0 = ONE ? a[0] : cmul(a[0], w[0]);
+        const C x1 = cmul(a[1], w[1]);
+        C s02, d02, s13, d13;
         bfly_w(x0, a[2], w[2], s02, d02);
         bfly_w(x1, a[3], w[3], s13, d13);
         finish(a, s02, d02, s13, d13);
     }
 };
 
-template <int R, typename T, int K = 0>
-__device__ __forceinline__ void combine_half(cx<T>* e, cx<T>* o, cx<T>* a) {
+template <int R, typename C, int K = 0>
+__device__ __forceinline__ void combine_half(C* e, C* o, C* a) {
     if constexpr (K < R / 2) {
         bfly<R, K>(e[K], o[K], a[K], a[K + R / 2]);
-        combine_half<R, T, K + 1>(e, o, a);
+        combine_half<R, C, K + 1>(e, o, a);
     }
 }
 
-template <int R, typename T> struct Dft {
+template <int R, typename C> struct Dft {
     static_assert(R % 2 == 0, "odd codelet sizes other than 3 are not provided");
-    __device__ __forceinline__ static void run(cx<T>* a) {
-        cx<T> e[R / 2], o[R / 2];
+    __device__ __forceinline__ static void run(C* a) {
+        C e[R / 2], o[R / 2];
 #pragma unroll
         for (int i = 0; i < R / 2; ++i) {
             e[i] = a[2 * i];
             o[i] = a[2 * i + 1];
         }
-        Dft<R / 2, T>::run(e);
-        Dft<R / 2, T>::run(o);
-        combine_half<R, T>(e, o, a);
+        Dft<R / 2, C>::run(e);
+        Dft<R / 2, C>::run(o);
+        combine_half<R, C>(e, o, a);
     }
-    template <bool ONE>
-    __device__ __forceinline__ static void run_tw(cx<T>* a, const cx<T>* w) {
-        cx<T> e[R / 2], o[R / 2], we[R / 2], wo[R / 2];
+    template <bool ONE, typename Wt>
+    __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
+        C e[R / 2], o[R / 2];
+        Wt we[R / 2], wo[R / 2];
 #pragma unroll
         for (int i = 0; i < R / 2; ++i) {
             e[i] = a[2 * i];
@@ -236,10 +217,19 @@ template <int R, typename T> struct Dft {
             we[i] = w[2 * i];
             wo[i] = w[2 * i + 1];
         }
-        Dft<R / 2, T>::template run_tw<ONE>(e, we);
-        Dft<R / 2, T>::template run_tw<false>(o, wo);
-        combine_half<R, T>(e, o, a);
+        Dft<R / 2, C>::template run_tw<ONE>(e, we);
+        Dft<R / 2, C>::template run_tw<false>(o, wo);
+        combine_half<R, C>(e, o, a);
     }
+};
+
+// stage twiddles of element type C: the table layout and one entry
+template <typename C> struct TwOf;
+template <typename T> struct TwOf<cx<T>> {
+    using tab = cx<T>;
+    using type = cx<T>;
+    __device__ __forceinline__ static cx<T> at(const cx<T>* tw, int i) { return ldg(&tw[i]); }
+    __device__ __forceinline__ static cx<T> one() { return mk(T(1), T(0)); }
 };
 
 // ---------------------------------------------------------------------------
@@ -248,11 +238,11 @@ template <int R, typename T> struct Dft {
 //   sbuf   : exchange buffer; sidx(m) maps sequence index m to its slot
 //   tw     : table W_N^m = exp(-2 pi i m / N), m < N (read-only path)
 //   sync() : barrier over all threads sharing sbuf
-// Inverse transforms are computed as conj(DFT(conj(x))) by the callers.
+// Plan::inv computes the inverse as conj(DFT(conj(x))).
 // ---------------------------------------------------------------------------
-template <typename T, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
-__device__ __forceinline__ void fft_stages(cx<T> (&v)[E], cx<T>* sbuf, int p,
-                                           const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
+template <typename C, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
+__device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
+                                           SIdx sidx, Sync sync) {
     constexpr int P = N / E;
     constexpr int Q = E / R;
     constexpr bool last = (sizeof...(Rest) == 0);
@@ -260,20 +250,20 @@ __device__ __forceinline__ void fft_stages(cx<T> (&v)[E], cx<T>* sbuf, int p,
 #pragma unroll
     for (int q = 0; q < Q; ++q) {
         const int j = p + q * P;
-        cx<T> a[R];
+        C a[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) a[r] = v[q + r * Q];
         int jm = 0;
         if constexpr (Ns > 1) {
             jm = j % Ns;
             constexpr int step = N / (Ns * R);
-            cx<T> w[R];
-            w[0] = mk(T(1), T(0));
+            typename TwOf<C>::type w[R];
+            w[0] = TwOf<C>::one();
 #pragma unroll
-            for (int r = 1; r < R; ++r) w[r] = ldg(&tw[r * jm * step]);
-            Dft<R, T>::template run_tw<true>(a, w);
+            for (int r = 1; r < R; ++r) w[r] = TwOf<C>::at(tw, r * jm * step);
+            Dft<R, C>::template run_tw<true>(a, w);
         } else {
-            Dft<R, T>::run(a);
+            Dft<R, C>::run(a);
         }
         if constexpr (last) {
 #pragma unroll
@@ -289,7 +279,7 @@ __device__ __forceinline__ void fft_stages(cx<T> (&v)[E], cx<T>* sbuf, int p,
 #pragma unroll
         for (int s = 0; s < E; ++s) v[s] = sbuf[sidx(p + s * P)];
         sync();
-        fft_stages<T, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
     }
 }
 
@@ -300,17 +290,17 @@ struct Plan {
     static constexpr int E = E_;
     static constexpr int P = N_ / E_;
     static constexpr int nstages = sizeof...(Rs);
-    template <typename T, typename SIdx, typename Sync>
-    __device__ __forceinline__ static void fwd(cx<T> (&v)[E_], cx<T>* sbuf, int p,
-                                               const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
-        fft_stages<T, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+    template <typename C, typename SIdx, typename Sync>
+    __device__ __forceinline__ static void fwd(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
+                                               SIdx sidx, Sync sync) {
+        fft_stages<C, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
     }
-    template <typename T, typename SIdx, typename Sync>
-    __device__ __forceinline__ static void inv(cx<T> (&v)[E_], cx<T>* sbuf, int p,
-                                               const cx<T>* __restrict__ tw, SIdx sidx, Sync sync) {
+    template <typename C, typename SIdx, typename Sync>
+    __device__ __forceinline__ static void inv(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
+                                               SIdx sidx, Sync sync) {
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
-        fft_stages<T, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
     }

@@ -481,12 +481,16 @@ constexpr int ZLINE_WARPS = 4;
 // A line group is the lanes that transform one z line: P = N/E lanes. With
 // P <= 32 a warp holds 32/P lines (GPW); with P = 64 (N = 1024) two warps hold
 // one line (GW = 2) and exchange through a named barrier.
-template <int N> constexpr int zline_gw() { return Plans<N>::A::P > 32 ? Plans<N>::A::P / 32 : 1; }
-template <int N> constexpr int zline_gpw() { return Plans<N>::A::P <= 32 ? 32 / Plans<N>::A::P : 1; }
+// the line kernel's plan: the y-pass plan (at 512^3 two warps per line with 8
+// elements per lane, 128 registers and twice the warps per SM, measured 8 %
+// slower than one warp with 16 elements)
+template <int N> struct ZPlan { using A = typename Plans<N>::A; };
+template <int N> constexpr int zline_gw() { return ZPlan<N>::A::P > 32 ? ZPlan<N>::A::P / 32 : 1; }
+template <int N> constexpr int zline_gpw() { return ZPlan<N>::A::P <= 32 ? 32 / ZPlan<N>::A::P : 1; }
 template <typename T, int N>
 constexpr bool zline_ok() {
-    constexpr int P = Plans<N>::A::P;
-    return sizeof(T) == 4 && Plans<N>::A::E <= 16 &&
+    constexpr int P = ZPlan<N>::A::P;
+    return sizeof(T) == 4 && ZPlan<N>::A::E <= 16 &&
            (P <= 32 ? (32 % P == 0 && ((long long)N * N) % (32 / P) == 0) : P == 64);
 }
 // With several lines per warp (N <= 256) the exchange buffers live in the
@@ -516,7 +520,7 @@ __global__ void __launch_bounds__(ZLINE_WARPS * 32)
 k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, int want_umax,
         int nmem) {
     using G = Geo<N>;
-    using PL = typename Plans<N>::A;
+    using PL = typename ZPlan<N>::A;
     constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>(), GW = zline_gw<N>(), GT = 32 * GW;
     constexpr int NGRP = zline_groups<N>();
     constexpr int NZP = G::NZP;
@@ -730,6 +734,32 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         const cx<T>* src = W + (long long)c * G::FS + off;
 #pragma unroll
         for (int s = 0; s < E; ++s) F[c][s] = colok ? src[(long long)(p + P * s) * xs] : czero<T>();
+    }
+    if constexpr (MODE <= X_STAGE4) {
+        // The epilogue reads the state of each of its modes after the FFT. Its
+        // rows (TT modes of one x row, per array and component: one 16-byte
+        // aligned segment each) are prefetched into L2 now, spread over the
+        // TT threads of a row, so that those loads hit L2.
+        const int rem0 = G::KC2 - ky * ky - kz0 * kz0;
+        const uint32_t seg = (uint32_t)((TT < G::NZP - kz0 ? TT : G::NZP - kz0) * sizeof(cx<T>));
+        constexpr bool kIF = INTEG == INT_IFRK4;
+        constexpr bool needU = !(kIF && MODE == X_STAGE4);
+        constexpr bool needA = INTEG != INT_TAB && MODE != X_STAGE1;
+        for (int s = t; s < E; s += TT) {
+            const int kx = kof<N>(p + P * s);
+            if (kx * kx > rem0) continue;
+            const long long q = (long long)(p + P * s) * xs + (long long)j * G::NZP + kz0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (needU) bulk_prefetch_l2(U + c * G::FS + q, seg);
+                if (needA) bulk_prefetch_l2(ACC + c * G::FS + q, seg);
+                if constexpr (INTEG == INT_TAB) {
+                    for (int jj = 0; jj < rs.nk && jj < 6; ++jj)
+                        if (rs.c[jj] != 0.0 || rs.e[jj] != 0.0)
+                            bulk_prefetch_l2(K + (long long)jj * 3 * G::FS + c * G::FS + q, seg);
+                }
+            }
+        }
     }
 #pragma unroll
     for (int c = 0; c < 3; ++c) PL::fwd(F[c], sbuf, p, tw, sidx, sync);

@@ -48,6 +48,11 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
         : "memory");
 }
 
+// bulk prefetch of global bytes into L2; src 16-byte aligned, bytes % 16 == 0
+__device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // 3D tiled tensor copy global -> shared (coordinates innermost first)
 __device__ __forceinline__ void tensor3_g2s(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
                                             uint64_t* bar) {
