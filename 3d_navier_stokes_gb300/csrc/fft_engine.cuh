@@ -68,6 +68,37 @@ __device__ constexpr double kS12[12] = {
 __device__ __forceinline__ float fmat(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmat(double a, double b, double c) { return fma(a, b, c); }
 
+// Element-wise complex add, subtract and broadcast FMA (c a.x + b.x, c a.y + b.y).
+// With PK and FP32 the real and imaginary parts go through one FP32x2
+// instruction (sm_100 and later; each lane rounds like the scalar instruction,
+// so results are unchanged). Kernels choose PK per plan: it saves issue slots
+// in the issue-bound z lines and the y passes, and costs registers elsewhere.
+template <bool PK, typename T> __device__ __forceinline__ cx<T> vadd(cx<T> a, cx<T> b) { return a + b; }
+template <bool PK, typename T> __device__ __forceinline__ cx<T> vsub(cx<T> a, cx<T> b) { return a - b; }
+template <bool PK, typename T> __device__ __forceinline__ cx<T> vfma(T c, cx<T> a, cx<T> b) {
+    return mk(fmat(c, a.x, b.x), fmat(c, a.y, b.y));
+}
+__device__ __forceinline__ float2 f2of(cx<float> a) { return make_float2(a.x, a.y); }
+__device__ __forceinline__ cx<float> cxof(float2 a) { return mk(a.x, a.y); }
+__device__ __forceinline__ cx<float> vadd2(cx<float> a, cx<float> b) { return cxof(__fadd2_rn(f2of(a), f2of(b))); }
+__device__ __forceinline__ cx<float> vsub2(cx<float> a, cx<float> b) {
+    unsigned long long ra, rb, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(a.x), "f"(a.y));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(b.x), "f"(b.y));
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    cx<float> d;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(d.x), "=f"(d.y) : "l"(rd));
+    return d;
+}
+__device__ __forceinline__ cx<float> vfma2(float c, cx<float> a, cx<float> b) {
+    return cxof(__ffma2_rn(make_float2(c, c), f2of(a), f2of(b)));
+}
+template <> __device__ __forceinline__ cx<float> vadd<true, float>(cx<float> a, cx<float> b) { return vadd2(a, b); }
+template <> __device__ __forceinline__ cx<float> vsub<true, float>(cx<float> a, cx<float> b) { return vsub2(a, b); }
+template <> __device__ __forceinline__ cx<float> vfma<true, float>(float c, cx<float> a, cx<float> b) {
+    return vfma2(c, a, b);
+}
+
 // lo = e + w o, hi = e - w o for a runtime twiddle w: four FMAs form lo and
 // hi = 2e - lo takes two more (6 instructions instead of a complex product
 // and four additions; the absolute error stays within a rounding of |e| + |o|)
@@ -80,19 +111,19 @@ __device__ __forceinline__ void bfly_w(cx<T> e, cx<T> o, cx<T> w, cx<T>& lo, cx<
 // lo = e + W_R^K o, hi = e - W_R^K o with W_R = exp(-2 pi i / R): additions
 // only for the trivial angles, two additions and four FMAs for the odd
 // multiples of 45 degrees, four FMAs and the 2e - lo form otherwise.
-template <int R, int K, typename T>
+template <int R, int K, bool PK = false, typename T>
 __device__ __forceinline__ void bfly(cx<T> e, cx<T> o, cx<T>& lo, cx<T>& hi) {
     constexpr int k = K % R;
     if constexpr (k == 0) {
-        lo = e + o;
-        hi = e - o;
+        lo = vadd<PK>(e, o);
+        hi = vsub<PK>(e, o);
     } else if constexpr (4 * k == R) {
         const cx<T> t = mul_mi(o);
         lo = e + t;
         hi = e - t;
     } else if constexpr (2 * k == R) {
-        lo = e - o;
-        hi = e + o;
+        lo = vsub<PK>(e, o);
+        hi = vadd<PK>(e, o);
     } else if constexpr (4 * k == 3 * R) {
         const cx<T> t = mul_i(o);
         lo = e + t;
@@ -105,13 +136,13 @@ __device__ __forceinline__ void bfly(cx<T> e, cx<T> o, cx<T>& lo, cx<T>& hi) {
         const T c = T(cd), s = T(sd);
         // W o = (c o.x + s o.y, c o.y - s o.x)
         if constexpr (!tri && (8 * k) % R == 0 && cd == sd) {          // 1/8, 5/8 turn: (c u, c v)
-            const T u = o.x + o.y, v = o.y - o.x;
-            lo = mk(fmat(c, u, e.x), fmat(c, v, e.y));
-            hi = mk(fmat(-c, u, e.x), fmat(-c, v, e.y));
+            const cx<T> uv = mk(o.x + o.y, o.y - o.x);
+            lo = vfma<PK>(c, uv, e);
+            hi = vfma<PK>(-c, uv, e);
         } else if constexpr (!tri && (8 * k) % R == 0 && cd == -sd) {  // 3/8, 7/8 turn: (-c v, c u)
-            const T u = o.x + o.y, v = o.y - o.x;
-            lo = mk(fmat(-c, v, e.x), fmat(c, u, e.y));
-            hi = mk(fmat(c, v, e.x), fmat(-c, u, e.y));
+            const cx<T> vu = mk(o.x - o.y, o.x + o.y);                 // (-v, u)
+            lo = vfma<PK>(c, vu, e);
+            hi = vfma<PK>(-c, vu, e);
         } else {
             lo = mk(fmat(c, o.x, fmat(s, o.y, e.x)), fmat(c, o.y, fmat(-s, o.x, e.y)));
             hi = mk(fmat(T(2), e.x, -lo.x), fmat(T(2), e.y, -lo.y));
@@ -126,13 +157,13 @@ __device__ __forceinline__ void bfly(cx<T> e, cx<T> o, cx<T>& lo, cx<T>& hi) {
 //   run_tw<ONE>(a, w): X = DFT(a[r] w[r]), the stage twiddles folded into the
 //                   first butterfly level (w[0] is 1 and unread when ONE)
 // ---------------------------------------------------------------------------
-template <int R, typename C> struct Dft;   // C = cx<T>
+template <int R, typename C, bool PK = false> struct Dft;   // C = cx<T>
 
-template <typename C> struct Dft<1, C> {
+template <typename C, bool PK> struct Dft<1, C, PK> {
     __device__ __forceinline__ static void run(C*) {}
 };
-template <typename C> struct Dft<2, C> {
-    __device__ __forceinline__ static void run(C* a) { bfly<2, 0>(a[0], a[1], a[0], a[1]); }
+template <typename C, bool PK> struct Dft<2, C, PK> {
+    __device__ __forceinline__ static void run(C* a) { bfly<2, 0, PK>(a[0], a[1], a[0], a[1]); }
     template <bool ONE, typename Wt>
     __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
         const C x0 = ONE ? a[0] : cmul(a[0], w[0]);
@@ -144,7 +175,7 @@ template <typename C> struct RealOf;
 template <typename T> struct RealOf<cx<T>> { using type = T; };
 template <typename T> __device__ __forceinline__ cx<T> mi_scale(cx<T> d, T h) { return mk(d.y * h, -d.x * h); }
 
-template <typename C> struct Dft<3, C> {
+template <typename C, bool PK> struct Dft<3, C, PK> {
     using T = typename RealOf<C>::type;
     __device__ __forceinline__ static void run(C* a) {
         const T h = T(0.86602540378443864676);
@@ -163,15 +194,15 @@ template <typename C> struct Dft<3, C> {
         run(a);
     }
 };
-template <typename C> struct Dft<4, C> {
+template <typename C, bool PK> struct Dft<4, C, PK> {
     __device__ __forceinline__ static void finish(C* a, C s02, C d02, C s13, C d13) {
-        bfly<4, 0>(s02, s13, a[0], a[2]);
-        bfly<4, 1>(d02, d13, a[1], a[3]);   // d02 -/+ i d13
+        bfly<4, 0, PK>(s02, s13, a[0], a[2]);
+        bfly<4, 1, PK>(d02, d13, a[1], a[3]);   // d02 -/+ i d13
     }
     __device__ __forceinline__ static void run(C* a) {
         C s02, d02, s13, d13;
-        bfly<2, 0>(a[0], a[2], s02, d02);
-        bfly<2, 0>(a[1], a[3], s13, d13);
+        bfly<2, 0, PK>(a[0], a[2], s02, d02);
+        bfly<2, 0, PK>(a[1], a[3], s13, d13);
         finish(a, s02, d02, s13, d13);
     }
     template <bool ONE, typename Wt>
@@ -185,15 +216,15 @@ template <typename C> struct Dft<4, C> {
     }
 };
 
-template <int R, typename C, int K = 0>
+template <int R, typename C, bool PK, int K = 0>
 __device__ __forceinline__ void combine_half(C* e, C* o, C* a) {
     if constexpr (K < R / 2) {
-        bfly<R, K>(e[K], o[K], a[K], a[K + R / 2]);
-        combine_half<R, C, K + 1>(e, o, a);
+        bfly<R, K, PK>(e[K], o[K], a[K], a[K + R / 2]);
+        combine_half<R, C, PK, K + 1>(e, o, a);
     }
 }
 
-template <int R, typename C> struct Dft {
+template <int R, typename C, bool PK> struct Dft {
     static_assert(R % 2 == 0, "odd codelet sizes other than 3 are not provided");
     __device__ __forceinline__ static void run(C* a) {
         C e[R / 2], o[R / 2];
@@ -202,9 +233,9 @@ template <int R, typename C> struct Dft {
             e[i] = a[2 * i];
             o[i] = a[2 * i + 1];
         }
-        Dft<R / 2, C>::run(e);
-        Dft<R / 2, C>::run(o);
-        combine_half<R, C>(e, o, a);
+        Dft<R / 2, C, PK>::run(e);
+        Dft<R / 2, C, PK>::run(o);
+        combine_half<R, C, PK>(e, o, a);
     }
     template <bool ONE, typename Wt>
     __device__ __forceinline__ static void run_tw(C* a, const Wt* w) {
@@ -217,9 +248,9 @@ template <int R, typename C> struct Dft {
             we[i] = w[2 * i];
             wo[i] = w[2 * i + 1];
         }
-        Dft<R / 2, C>::template run_tw<ONE>(e, we);
-        Dft<R / 2, C>::template run_tw<false>(o, wo);
-        combine_half<R, C>(e, o, a);
+        Dft<R / 2, C, PK>::template run_tw<ONE>(e, we);
+        Dft<R / 2, C, PK>::template run_tw<false>(o, wo);
+        combine_half<R, C, PK>(e, o, a);
     }
 };
 
@@ -240,7 +271,7 @@ template <typename T> struct TwOf<cx<T>> {
 //   sync() : barrier over all threads sharing sbuf
 // Plan::inv computes the inverse as conj(DFT(conj(x))).
 // ---------------------------------------------------------------------------
-template <typename C, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
+template <typename C, bool PK, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
 __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                            SIdx sidx, Sync sync) {
     constexpr int P = N / E;
@@ -261,9 +292,9 @@ __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const type
             w[0] = TwOf<C>::one();
 #pragma unroll
             for (int r = 1; r < R; ++r) w[r] = TwOf<C>::at(tw, r * jm * step);
-            Dft<R, C>::template run_tw<true>(a, w);
+            Dft<R, C, PK>::template run_tw<true>(a, w);
         } else {
-            Dft<R, C>::run(a);
+            Dft<R, C, PK>::run(a);
         }
         if constexpr (last) {
 #pragma unroll
@@ -279,7 +310,7 @@ __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const type
 #pragma unroll
         for (int s = 0; s < E; ++s) v[s] = sbuf[sidx(p + s * P)];
         sync();
-        fft_stages<C, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
     }
 }
 
@@ -290,17 +321,18 @@ struct Plan {
     static constexpr int E = E_;
     static constexpr int P = N_ / E_;
     static constexpr int nstages = sizeof...(Rs);
-    template <typename C, typename SIdx, typename Sync>
+    // PK: FP32x2 additions in the butterflies (see vadd)
+    template <bool PK = false, typename C, typename SIdx, typename Sync>
     __device__ __forceinline__ static void fwd(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                                SIdx sidx, Sync sync) {
-        fft_stages<C, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
     }
-    template <typename C, typename SIdx, typename Sync>
+    template <bool PK = false, typename C, typename SIdx, typename Sync>
     __device__ __forceinline__ static void inv(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                                SIdx sidx, Sync sync) {
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
-        fft_stages<C, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
     }

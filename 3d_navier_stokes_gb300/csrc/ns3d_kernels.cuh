@@ -283,8 +283,8 @@ k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
         if (INV) in = in && (ky * ky <= rem);
         v[s] = in ? base[(long long)jj * G::NZP] : czero<T>();
     }
-    if (INV) PL::inv(v, sbuf, p, tw, sidx, sync);
-    else PL::fwd(v, sbuf, p, tw, sidx, sync);
+    if (INV) PL::template inv<true>(v, sbuf, p, tw, sidx, sync);
+    else PL::template fwd<true>(v, sbuf, p, tw, sidx, sync);
     if (colok) {
 #pragma unroll
         for (int s = 0; s < E; ++s) {
@@ -516,12 +516,16 @@ template <typename T, int N> constexpr size_t zline_smem() {
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(ZLINE_WARPS * 32)
+__global__ void __launch_bounds__(ZLINE_WARPS * 32, zline_xbuf_in_stage<N>() ? 3 : 2)
 k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, int want_umax,
         int nmem) {
     using G = Geo<N>;
     using PL = typename ZPlan<N>::A;
     constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>(), GW = zline_gw<N>(), GT = 32 * GW;
+    // FP32x2 butterfly additions where one line fills one warp (512 points; 4 %
+    // faster there); the 256-point lines of two per warp need the registers for
+    // three CTAs per SM, and the two-warp lines of 1024 points keep the scalar form
+    constexpr bool kPK = GPW == 1 && GW == 1;
     constexpr int NGRP = zline_groups<N>();
     constexpr int NZP = G::NZP;
     constexpr long long NG = (long long)N * N / GPW;   // work items (line groups) per ensemble member
@@ -613,7 +617,9 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
             for (int q = 0; q < E; ++q) {
                 const int m = p + P * q;
                 cx<T> z = czero<T>();
-                if (m == 0) {
+                if (P * q > G::KC && P * q + P - 1 < N - G::KC) {
+                    // every lane's mode of this slot is outside the kept band
+                } else if (m == 0) {
                     z = mk(A[0].x, B[0].x);
                 } else if (m <= G::KC) {
                     const cx<T> a = A[m], b = B[m];
@@ -631,9 +637,9 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         load_pair(2, V2);
         load_pair(4, V3);
         sync();   // every lane has read the staged lines before the buffer is reused
-        PL::inv(V1, sb, p, tw, sidx, sync);
-        PL::inv(V2, sb, p, tw, sidx, sync);
-        PL::inv(V3, sb, p, tw, sidx, sync);
+        PL::template inv<kPK>(V1, sb, p, tw, sidx, sync);
+        PL::template inv<kPK>(V2, sb, p, tw, sidx, sync);
+        PL::template inv<kPK>(V3, sb, p, tw, sidx, sync);
 #pragma unroll
         for (int q = 0; q < E; ++q) {
             const T ux = V1[q].x, uy = V1[q].y, uz = V2[q].x;
@@ -643,9 +649,10 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
             V2[q] = mk(ux * wy - uy * wx, T(0));
         }
         // Nx + i Ny -> two spectra through the exchange buffer
-        PL::fwd(V1, sb, p, tw, sidx, sync);
+        PL::template fwd<kPK>(V1, sb, p, tw, sidx, sync);
 #pragma unroll
-        for (int q = 0; q < E; ++q) sb[sidx(p + P * q)] = V1[q];
+        for (int q = 0; q < E; ++q)   // only the slots read below: m <= KC and N - m
+            if (P * q <= G::KC || P * q + P - 1 >= N - G::KC) sb[sidx(p + P * q)] = V1[q];
         sync();
         {
             cx<T>* outA = Wm + line * NZP;
@@ -665,12 +672,12 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         }
         sync();
         // Nz (real input): its spectrum is the transform itself
-        PL::fwd(V2, sb, p, tw, sidx, sync);
+        PL::template fwd<kPK>(V2, sb, p, tw, sidx, sync);
         cx<T>* outC = Wm + 2 * G::FS + line * NZP;
 #pragma unroll
         for (int q = 0; q < E; ++q) {
             const int m = p + P * q;
-            if (m <= G::KC) outC[m] = V2[q];
+            if (P * q <= G::KC && m <= G::KC) outC[m] = V2[q];
         }
         // the stage buffer is refilled by a bulk copy (async proxy) next iteration:
         // order every lane's exchange accesses to it before that
