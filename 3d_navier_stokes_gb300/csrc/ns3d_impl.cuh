@@ -125,7 +125,7 @@ class Impl final : public Base {
         }
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
         // opt-in shared memory sizes
-        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x()));
+        NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_xi()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
@@ -152,6 +152,7 @@ class Impl final : public Base {
     // ---------------------------------------------------------------- passes
     static constexpr size_t smem_a() { return sizeof(cx<T>) * (size_t)N * TA; }
     static constexpr size_t smem_x() { return sizeof(cx<T>) * (size_t)N * TX; }
+    static constexpr size_t smem_xi() { return xinv_smem<T, N, V>(); }
     static constexpr size_t smem_z() {
         return sizeof(cx<T>) * (size_t)ZP * 3 * zpad<N>() + sizeof(T) * (size_t)ZP * 12 * N;
     }
@@ -168,7 +169,7 @@ class Impl final : public Base {
 
     // each launcher covers members [m0, m0 + cnt); `in` points at member 0's arrays
     void p1(const cx<T>* in, int m0, int cnt) {
-        k_xinv<T, N, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
+        k_xinv<T, N, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_xi(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
     }
     void p2(int m0, int cnt) {
         k_ypass<T, N, true, V><<<dim3(NTA, N, 6 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
