@@ -315,12 +315,14 @@ __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const type
 }
 
 // A compile-time FFT plan: length N, E elements per thread, radices Rs...
+template <int R, int... Rest> struct FirstOf { static constexpr int value = R; };
 template <int N_, int E_, int... Rs>
 struct Plan {
     static constexpr int N = N_;
     static constexpr int E = E_;
     static constexpr int P = N_ / E_;
     static constexpr int nstages = sizeof...(Rs);
+    static constexpr int R1 = FirstOf<Rs...>::value;   // radix of the first stage
     // PK: FP32x2 additions in the butterflies (see vadd)
     template <bool PK = false, typename C, typename SIdx, typename Sync>
     __device__ __forceinline__ static void fwd(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,

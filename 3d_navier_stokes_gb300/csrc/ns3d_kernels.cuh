@@ -120,10 +120,23 @@ template <int N> constexpr int zpairs() {
 struct SyncBlock {
     __device__ __forceinline__ void operator()() const { __syncthreads(); }
 };
-template <int TT>
-struct StridedIdx {   // exchange slot of element m of pencil t: [m][TT]
+// Exchange slot of element m of pencil t: [m'][TT] with the row m' = m XOR
+// ((m / R1) mod G), G = 32 / TT pencil groups per warp (G < R1, power-of-two
+// R1; identity otherwise). The first stage's writes of a warp's G groups go
+// to rows R1 apart (R1 * TT complex, a multiple of 128 bytes) and would share
+// one bank range; the XOR spreads them over the banks. The reads of
+// consecutive rows stay consecutive (a permutation inside each aligned block
+// of R1 rows), so neither side has bank conflicts.
+template <int TT, int R1 = 1>
+struct StridedIdx {
+    static constexpr int G = TT < 16 ? 32 / TT : 1;
+    static constexpr bool kSwz = G > 1 && (R1 & (R1 - 1)) == 0 && R1 >= G;
+    static constexpr int kShift = (R1 >= 16) ? 4 : (R1 >= 8) ? 3 : (R1 >= 4) ? 2 : (R1 >= 2) ? 1 : 0;
     int t;
-    __device__ __forceinline__ int operator()(int m) const { return m * TT + t; }
+    __device__ __forceinline__ int operator()(int m) const {
+        if constexpr (kSwz) m ^= (m >> kShift) & (G - 1);
+        return m * TT + t;
+    }
 };
 struct PaddedIdx {    // exchange slot of element m of one line: one pad slot per 16
     __device__ __forceinline__ int operator()(int m) const { return m + (m >> 4); }
@@ -210,7 +223,7 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     const long long off = (long long)j * G::NZP + kz;
     const long long xs = (long long)N * G::NZP;
     const T scale = T(1) / (T(N) * T(N) * T(N));
-    StridedIdx<TT> sidx{t};
+    StridedIdx<TT, PL::R1> sidx{t};
     SyncBlock sync;
 
     constexpr bool kStage = TileVar<V>::STAGE;
@@ -338,7 +351,7 @@ k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     constexpr int NF = INV ? 6 : 3;
     const long long fld = (long long)(blockIdx.z / NF) * 6 + blockIdx.z % NF;
     cx<T>* base = W + fld * G::FS + (long long)blockIdx.y * N * G::NZP + kz;
-    StridedIdx<TT> sidx{t};
+    StridedIdx<TT, PL::R1> sidx{t};
     SyncBlock sync;
     cx<T> v[E];
 #pragma unroll
@@ -798,7 +811,7 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
     const long long off = (long long)j * G::NZP + kz;
     const long long xs = (long long)N * G::NZP;
-    StridedIdx<TT> sidx{t};
+    StridedIdx<TT, PL::R1> sidx{t};
     SyncBlock sync;
 
     cx<T> F[3][E];
