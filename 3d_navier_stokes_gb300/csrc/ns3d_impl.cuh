@@ -41,6 +41,8 @@ class Impl final : public Base {
     static constexpr int TX = tile_x<T, N, V>();
     static constexpr int ZP = zpairs<N>();
     static constexpr int NTA = (G::NZ1 + TA - 1) / TA;
+    static constexpr int TAF = tile_a<T, N, V, false>();   // forward y pass
+    static constexpr int NTAF = (G::NZ1 + TAF - 1) / TAF;
     static constexpr int NTX = (G::NZ1 + TX - 1) / TX;
     static constexpr int LPC = meas_lines_per_cta<N>();
     static constexpr long long NMEAS = ((long long)N * G::NKY + LPC - 1) / LPC;
@@ -127,7 +129,7 @@ class Impl final : public Base {
         // opt-in shared memory sizes
         NS3D_CK(cudaFuncSetAttribute(k_xinv<T, N, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_xi()));
         NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, true, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
-        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_a()));
+        NS3D_CK(cudaFuncSetAttribute(k_ypass<T, N, false, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_af()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         if constexpr (zline_ok<T, N>()) {
             NS3D_CK(cudaFuncSetAttribute(k_zline<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_zl()));
@@ -151,6 +153,7 @@ class Impl final : public Base {
 
     // ---------------------------------------------------------------- passes
     static constexpr size_t smem_a() { return sizeof(cx<T>) * (size_t)N * TA; }
+    static constexpr size_t smem_af() { return sizeof(cx<T>) * (size_t)N * TAF; }
     static constexpr size_t smem_x() { return sizeof(cx<T>) * (size_t)N * TX; }
     static constexpr size_t smem_xi() { return xinv_smem<T, N, V>(); }
     static constexpr size_t smem_z() {
@@ -202,7 +205,7 @@ class Impl final : public Base {
     int zform() const override { return zform_; }
     int variant() const override { return V; }
     void p4(int m0, int cnt) {
-        k_ypass<T, N, false, V><<<dim3(NTA, N, 3 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+        k_ypass<T, N, false, V><<<dim3(NTAF, N, 3 * cnt), TAF * PA::P, smem_af(), s_>>>(Wm(m0), tw_);
     }
     template <int INTEG, int MODE>
     void p5x(int m0, int cnt, cx<T>* out) {

@@ -74,6 +74,7 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 #ifndef NS3D_TILE_X32
 #define NS3D_TILE_X32 16
 #endif
+// A / AF: pencils per CTA of the inverse / forward y pass; X: of the x passes.
 // MINB / MINB_XI: CTAs per SM the x-forward / x-inverse passes are compiled
 // for (registers capped to fit); BATCH: the x-forward epilogue issues all of a
 // thread's state loads of a component before their updates (more registers);
@@ -81,12 +82,12 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 // (two live arrays instead of four; 11 % faster at 256^3, 2 % slower with the
 // 16-element plan of variant 3 at 512^3)
 template <int V> struct TileVar;
-template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<1> { static constexpr int A = 4, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<2> { static constexpr int A = 16, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, X = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = false; };
-template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false, STAGE = true; };
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<1> { static constexpr int A = 4, AF = 4, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<2> { static constexpr int A = 16, AF = 16, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, AF = 16, X = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = false; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false, STAGE = true; };
 
 // Variant 5: the default tiles and plans with the x-forward pass compiled for
 // two CTAs per SM, so one CTA's FFT overlaps another's loads (the x-inverse
@@ -105,8 +106,9 @@ template <int N, int V> struct PlansV {
     using X = typename std::conditional<(V == 3), typename AltX<N>::X, typename Plans<N>::X>::type;
 };
 template <int P, int W> constexpr int clip_tile() { return P * W <= 512 ? W : (P * 8 <= 512 ? 8 : (P * 4 <= 512 ? 4 : 2)); }
-template <typename T, int N, int V = 0> constexpr int tile_a() {
-    return sizeof(T) == 4 ? clip_tile<Plans<N>::A::P, TileVar<V>::A>() : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
+template <typename T, int N, int V = 0, bool INV = true> constexpr int tile_a() {
+    return sizeof(T) == 4 ? clip_tile<Plans<N>::A::P, (INV ? TileVar<V>::A : TileVar<V>::AF)>()
+                          : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
 }
 template <typename T, int N, int V = 0> constexpr int tile_x() {
     constexpr int P = PlansV<N, V>::X::P;
@@ -334,12 +336,14 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // Forward: inputs every y, outputs only where ky^2 + kz^2 <= KC^2.
 // ---------------------------------------------------------------------------
 template <typename T, int N, bool INV, int V = 0>
-__global__ void __launch_bounds__(tile_a<T, N, V>() * Plans<N>::A::P,
-                                  (1024 / (tile_a<T, N, V>() * Plans<N>::A::P) > 0 ? 1024 / (tile_a<T, N, V>() * Plans<N>::A::P) : 1))
+__global__ void __launch_bounds__(tile_a<T, N, V, INV>() * Plans<N>::A::P,
+                                  (1024 / (tile_a<T, N, V, INV>() * Plans<N>::A::P) > 0
+                                       ? 1024 / (tile_a<T, N, V, INV>() * Plans<N>::A::P)
+                                       : 1))
 k_ypass(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw) {
     using G = Geo<N>;
     using PL = typename Plans<N>::A;
-    constexpr int TT = tile_a<T, N, V>();
+    constexpr int TT = tile_a<T, N, V, INV>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);

@@ -228,3 +228,22 @@ def test_large_grid_properties(ns3d, N):
         p0 = u[:, :, 0]
         pm = np.conj(p0[(-np.arange(N)) % N][:, (-np.arange(N)) % N])
         assert np.abs(p0 - pm).max() < 1e-5 * np.abs(u).max()
+
+
+def test_fp32_512_tracks_fp64(ns3d):
+    """The 512^3 FP32 step (one-warp z lines with FP32x2 butterfly additions, the
+    tuned x-pass plan) against the FP64 engine over 3 forced steps from the same
+    state: total energy to 1e-6 and every shell of E(k) to 1e-6 of its maximum."""
+    N = 512
+    res = {}
+    for prec in ("fp64", "fp32"):
+        s = ns3d.Solver(N, nu=1e-3, dt=1e-3, precision=prec, forcing="SHELL", force_k=2)
+        s.InitialConditions("SPECTRUM", seed=0, k0=4.0)
+        s.RK4Step(3)
+        tot, Ek, _ = s.ComputeSystemMeasurables()
+        res[prec] = (tot["energy"], np.asarray(Ek))
+        del s
+    e64, k64 = res["fp64"]
+    e32, k32 = res["fp32"]
+    assert abs(e32 - e64) < 1e-6 * e64
+    assert np.max(np.abs(k32 - k64)) < 1e-6 * k64.max()
