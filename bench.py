@@ -47,7 +47,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256", "closure-infer"])
+    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256", "closure-infer", "integrators"])
     ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
     ap.add_argument("--les-steps", type=int, default=2000)
@@ -504,6 +504,46 @@ def run_decay(args, local):
     print(json.dumps(line), flush=True)
 
 
+def run_rk5(args, local):
+    """The integrators of the step at N^3 (default 512^3) FP32 with shell forcing: IF-RK4,
+    RK4CN (CFL 0.5), RK5CN (CFL 0.5, 6 RHS per step) and DP5CN (Dormand-Prince step
+    control, 7 RHS per attempt); per integrator the device time per step (CUDA events of the
+    library over --steps steps after --warmup) and the simulated time advanced per second."""
+    import importlib
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    # the shipped GB300 tuning table (the shapes bench's own tuning pass picks)
+    pkg.tuning_load(os.path.join(ROOT, "3d_navier_stokes_gb300", "tuning", "gb300.txt"))
+    N = args.N
+    out = {}
+    for integ in ("ifrk4", "rk4cn", "rk5cn", "dp5cn"):
+        s = pkg.Solver(N, nu=4e-4 if N >= 1024 else 1e-3, dt=1e-3, cfl=0.0 if integ == "dp5cn" else 0.5,
+                       precision="fp32", forcing="SHELL", force_k=2, integrator=integ, device=local)
+        s.InitialConditions("SPECTRUM", seed=0, k0=4.0)
+        s.RK4Step(args.warmup)
+        t0 = s.get_time()[0]
+        s.RK4Step(args.steps)
+        ms = s.last_step_ms()
+        t1, dt, _ = s.get_time()
+        rec = {"ms_per_step": ms / args.steps, "grid_pt_steps_per_s": N ** 3 * args.steps / (ms * 1e-3),
+               "sim_time_per_s": (t1 - t0) / (ms * 1e-3), "mean_dt": (t1 - t0) / args.steps,
+               "kernels_per_step": s.kernels_per_step}
+        if integ == "dp5cn":
+            err, rej = s.dp_stats()
+            rec["rejected_attempts"] = rej
+        out[integ] = rec
+        s.close()
+    line = {"metric": f"grid-pt*steps/s per integrator ({N}^3, FP32 bulk, forced turbulence)",
+            "value": out["rk5cn"]["grid_pt_steps_per_s"], "unit": "grid-pt*steps/s (RK5CN)",
+            "higher_is_better": True, "steps": args.steps, "warmup": args.warmup, "n_gpus": 1,
+            "data": "synthetic", "dtype": "f32", "integrators": out,
+            "config": {"workload": "integrators", "N": N, "nu": 4e-4 if N >= 1024 else 1e-3, "cfl": 0.5,
+                       "forcing": "shell k<=2", "k0": 4.0, "seed": 0, "dp5cn_tolerances": "1e-7 abs, 1e-7 rel"}}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -521,6 +561,9 @@ def main():
         return
     if args.workload == "closure-infer":
         run_closure_infer(args, local)
+        return
+    if args.workload == "integrators":
+        run_rk5(args, local)
         return
     run_ours(args, ws, rank, local)
 
