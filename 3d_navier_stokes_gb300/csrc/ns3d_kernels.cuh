@@ -947,8 +947,105 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         return;
     }
     double es[3] = {0.0, 0.0, 0.0};   // DP5CN error partial sums
+    if constexpr (INTEG == INT_TAB) {
+        // RK5 family: the projection of every mode of this thread first; then, in
+        // chunks of CH modes and per component, each stored stage's loads for all
+        // modes of the chunk before their sums (the stage and coefficient tests
+        // are uniform), so that a chunk's loads of one array are in flight at
+        // once. Each component's sums run in mode order, as in the per-mode form.
+        constexpr int CH = E < 4 ? E : (E >= 16 ? 2 : 4);
+        unsigned valid = 0u;
+        int k2s[E];
 #pragma unroll
-    for (int s = 0; s < E; ++s) {
+        for (int s = 0; s < E; ++s) {
+            const int i = p + P * s;
+            const int kx = kof<N>(i);
+            k2s[s] = 0;
+            if (!colok || kx * kx > rem) continue;
+            valid |= 1u << s;
+            const int k2 = kx * kx + ky * ky + kz * kz;
+            k2s[s] = k2;
+            cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
+            if (sgs && sd->sgs_on) {
+                const long long q = (long long)i * xs + off;
+                n0 = n0 + sgs[q];
+                n1 = n1 + sgs[G::FS + q];
+                n2 = n2 + sgs[2 * G::FS + q];
+            }
+            if (k2 > 0) {
+                const T kinv = T(1) / T(k2);
+                const cx<T> kdn = n0 * T(kx) + n1 * T(ky) + n2 * T(kz);
+                n0 = n0 - kdn * (T(kx) * kinv);
+                n1 = n1 - kdn * (T(ky) * kinv);
+                n2 = n2 - kdn * (T(kz) * kinv);
+            } else {
+                n0 = n1 = n2 = czero<T>();
+            }
+            F[0][s] = n0;
+            F[1][s] = n1;
+            F[2][s] = n2;
+        }
+#pragma unroll
+        for (int s0 = 0; s0 < E; s0 += CH) {
+            if (!((valid >> s0) & ((1u << CH) - 1u))) continue;
+            cx<T> ab[CH];
+#pragma unroll
+            for (int s = 0; s < CH; ++s) ab[s] = ldg(&tab[k2s[s0 + s]]);
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                cx<T> acc[CH], ea[CH];
+#pragma unroll
+                for (int s = 0; s < CH; ++s) {
+                    acc[s] = F[c][s0 + s] * T(rs.c_cur);
+                    ea[s] = F[c][s0 + s] * T(rs.e_cur);
+                }
+#pragma unroll
+                for (int jj = 0; jj < 6; ++jj) {
+                    if (jj < rs.nk && (rs.c[jj] != 0.0 || rs.e[jj] != 0.0)) {
+                        cx<T> kv[CH];
+#pragma unroll
+                        for (int s = 0; s < CH; ++s) {
+                            kv[s] = czero<T>();
+                            if ((valid >> (s0 + s)) & 1u)
+                                kv[s] = K[(long long)jj * 3 * G::FS + c * G::FS + (long long)(p + P * (s0 + s)) * xs + off];
+                        }
+#pragma unroll
+                        for (int s = 0; s < CH; ++s) {
+                            acc[s] = acc[s] + kv[s] * T(rs.c[jj]);
+                            ea[s] = ea[s] + kv[s] * T(rs.e[jj]);
+                        }
+                    }
+                }
+                cx<T> u[CH];
+#pragma unroll
+                for (int s = 0; s < CH; ++s) {
+                    u[s] = czero<T>();
+                    if ((valid >> (s0 + s)) & 1u) u[s] = U[c * G::FS + (long long)(p + P * (s0 + s)) * xs + off];
+                }
+#pragma unroll
+                for (int s = 0; s < CH; ++s) {
+                    if (!((valid >> (s0 + s)) & 1u)) continue;
+                    const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
+                    if (rs.store >= 0) K[(long long)rs.store * 3 * G::FS + q] = F[c][s0 + s];
+                    if (rs.kind == 0) {
+                        UT[q] = u[s] + acc[s] * h;
+                    } else if (rs.kind == 1) {
+                        U[q] = u[s] * ab[s].x + acc[s] * ab[s].y;
+                    } else {
+                        const cx<T> un = u[s] * ab[s].x + acc[s] * ab[s].y;
+                        ACC[q] = un;
+                        const cx<T> df = ea[s] * ab[s].y;
+                        const double m0 = sqrt((double)u[s].x * u[s].x + (double)u[s].y * u[s].y);
+                        const double m1 = sqrt((double)un.x * un.x + (double)un.y * un.y);
+                        const double den = sd->dp_atol + (m0 > m1 ? m0 : m1) * sd->dp_rtol;
+                        es[c] += ((double)df.x * df.x + (double)df.y * df.y) / (den * den);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int s = 0; s < (INTEG == INT_TAB ? 0 : E); ++s) {
         const int i = p + P * s;
         const int kx = kof<N>(i);
         if (!colok || kx * kx > rem) continue;
