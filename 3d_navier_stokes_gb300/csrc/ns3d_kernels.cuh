@@ -860,15 +860,17 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     const int rem = G::KC2 - ky * ky - kz * kz;
     if constexpr ((INTEG == INT_IFRK4 || INTEG == INT_RK4CN) && MODE <= X_STAGE4 && TileVar<V>::BATCH) {
         // RK4-family stages: the projection of every mode of this thread first,
-        // then per component all of its state loads before their updates, so
-        // that E loads (per array) are in flight at once
+        // then, in chunks of up to 8 modes and per component, the chunk's state
+        // loads before their updates, so that a chunk's loads (per array) are in
+        // flight at once
+        constexpr int CH = E > 8 ? 8 : E;
         unsigned valid = 0u;
-        cx<T> tb[E];
+        int k2s[E];
 #pragma unroll
         for (int s = 0; s < E; ++s) {
             const int i = p + P * s;
             const int kx = kof<N>(i);
-            tb[s] = czero<T>();
+            k2s[s] = 0;
             if (kx * kx > rem) continue;
             valid |= 1u << s;
             const int k2 = kx * kx + ky * ky + kz * kz;
@@ -892,28 +894,34 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
             F[0][s] = n0;
             F[1][s] = n1;
             F[2][s] = n2;
-            tb[s] = ldg(&tab[k2]);
+            k2s[s] = k2;
         }
         constexpr bool kIF = INTEG == INT_IFRK4;
         constexpr bool needU = !(kIF && MODE == X_STAGE4);
         constexpr bool needA = kIF ? (MODE != X_STAGE1) : (MODE != X_STAGE1);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            cx<T> u[E], a[E];
+        for (int s0 = 0; s0 < E; s0 += CH) {
+          if (!((valid >> s0) & ((1u << CH) - 1u))) continue;
+          cx<T> tb[CH];
 #pragma unroll
-            for (int s = 0; s < E; ++s) {
+          for (int s = 0; s < CH; ++s) tb[s] = ldg(&tab[k2s[s0 + s]]);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            cx<T> u[CH], a[CH];
+#pragma unroll
+            for (int s = 0; s < CH; ++s) {
                 u[s] = czero<T>();
                 a[s] = czero<T>();
-                if (!((valid >> s) & 1u)) continue;
-                const long long q = c * G::FS + (long long)(p + P * s) * xs + off;
+                if (!((valid >> (s0 + s)) & 1u)) continue;
+                const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
                 if (needU) u[s] = U[q];
                 if (needA) a[s] = ACC[q];
             }
 #pragma unroll
-            for (int s = 0; s < E; ++s) {
-                if (!((valid >> s) & 1u)) continue;
-                const long long q = c * G::FS + (long long)(p + P * s) * xs + off;
-                const cx<T> nn = F[c][s];
+            for (int s = 0; s < CH; ++s) {
+                if (!((valid >> (s0 + s)) & 1u)) continue;
+                const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
+                const cx<T> nn = F[c][s0 + s];
                 if constexpr (kIF) {
                     const T Eh = tb[s].x, Ef = tb[s].y;
                     if (MODE == X_STAGE1) {
@@ -943,6 +951,7 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
                     }
                 }
             }
+          }
         }
         return;
     }
