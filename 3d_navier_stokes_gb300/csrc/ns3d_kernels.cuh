@@ -1409,23 +1409,26 @@ k_measure(const cx<T>* __restrict__ U, double nu, int vp, double* __restrict__ p
             double eu = 0, ew = 0;
             int bin = 0x7fffffff;
             if (in) {
+                // per-mode terms in the state's precision (FP32 products of FP32 modes,
+                // 10x cheaper than FP64 on this GPU), every sum in FP64
+                using R = T;
                 const long long idx = ((long long)i * N + j) * G::NZP + kz;
                 const cx<T> a0 = U[idx], a1 = U[G::FS + idx], a2 = U[2 * G::FS + idx];
-                const double ux = a0.x, uxi = a0.y, uy = a1.x, uyi = a1.y, uz = a2.x, uzi = a2.y;
-                const double fkx = kx, fky = ky, fkz = kz;
+                const R ux = a0.x, uxi = a0.y, uy = a1.x, uyi = a1.y, uz = a2.x, uzi = a2.y;
+                const R fkx = R(kx), fky = R(ky), fkz = R(kz);
                 // w = i k x u  ->  re(w) = -(k x u_im), im(w) = k x u_re
-                const double wxr = -(fky * uzi - fkz * uyi), wxi = fky * uz - fkz * uy;
-                const double wyr = -(fkz * uxi - fkx * uzi), wyi = fkz * ux - fkx * uz;
-                const double wzr = -(fkx * uyi - fky * uxi), wzi = fkx * uy - fky * ux;
-                const double cxr = -(fky * wzi - fkz * wyi), cxi = fky * wzr - fkz * wyr;
-                const double cyr = -(fkz * wxi - fkx * wzi), cyi = fkz * wxr - fkx * wzr;
-                const double czr = -(fkx * wyi - fky * wxi), czi = fkx * wyr - fky * wxr;
-                eu = ux * ux + uxi * uxi + uy * uy + uyi * uyi + uz * uz + uzi * uzi;
-                ew = wxr * wxr + wxi * wxi + wyr * wyr + wyi * wyi + wzr * wzr + wzi * wzi;
-                const double ec = cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi;
+                const R wxr = -(fky * uzi - fkz * uyi), wxi = fky * uz - fkz * uy;
+                const R wyr = -(fkz * uxi - fkx * uzi), wyi = fkz * ux - fkx * uz;
+                const R wzr = -(fkx * uyi - fky * uxi), wzi = fkx * uy - fky * ux;
+                const R cxr = -(fky * wzi - fkz * wyi), cxi = fky * wzr - fkz * wyr;
+                const R cyr = -(fkz * wxi - fkx * wzi), cyi = fkz * wxr - fkx * wzr;
+                const R czr = -(fkx * wyi - fky * wxi), czi = fkx * wyr - fky * wxr;
+                eu = double(ux * ux + uxi * uxi + uy * uy + uyi * uyi + uz * uz + uzi * uzi);
+                ew = double(wxr * wxr + wxi * wxi + wyr * wyr + wyi * wyi + wzr * wzr + wzi * wzi);
+                const double ec = double(cxr * cxr + cxi * cxi + cyr * cyr + cyi * cyi + czr * czr + czi * czi);
                 // helicity Re(u . conj(w)); the reference's Re(u . w) (solver.c:1227)
                 // is identically zero because u . (k x u) = 0 (defect D12, fixed)
-                const double hel = (ux * wxr + uxi * wxi) + (uy * wyr + uyi * wyi) + (uz * wzr + uzi * wzi);
+                const double hel = double((ux * wxr + uxi * wxi) + (uy * wyr + uyi * wyi) + (uz * wzr + uzi * wzi));
                 const double kk = (double)k2;
                 const double pre = nu * (vp == 2 ? kk * kk : kk);
                 const double m = (kz == 0) ? 1.0 : 2.0;
