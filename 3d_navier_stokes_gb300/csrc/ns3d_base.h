@@ -94,9 +94,10 @@ Base* make_f32_v2(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v3(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v4(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v5(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v6(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f64_v0(int N, const ns3d_params* ps, int M, cudaStream_t s);
 bool supported_n(int N);
-constexpr int kTileVariants = 6;   // TileVar<0..5>, PlansV (ns3d_kernels.cuh)
+constexpr int kTileVariants = 7;   // TileVar<0..6>, PlansV (ns3d_kernels.cuh)
 
 inline unsigned long long host_splitmix64(unsigned long long x) {
     unsigned long long z = x + 0x9E3779B97F4A7C15ull;

@@ -44,6 +44,8 @@ class Impl final : public Base {
     static constexpr int TAF = tile_a<T, N, V, false>();   // forward y pass
     static constexpr int NTAF = (G::NZ1 + TAF - 1) / TAF;
     static constexpr int NTX = (G::NZ1 + TX - 1) / TX;
+    static constexpr int TXF = tile_x<T, N, V, true>();   // forward x pass
+    static constexpr int NTXF = (G::NZ1 + TXF - 1) / TXF;
     static constexpr int LPC = meas_lines_per_cta<N>();
     static constexpr long long NMEAS = ((long long)N * G::NKY + LPC - 1) / LPC;
     static constexpr int MWIDTH = 5 + 2 * G::NSP;
@@ -101,7 +103,7 @@ class Impl final : public Base {
             // stored stages k_1..k_6 of the RK5 family, and the DP5CN error partial sums
             NS3D_CK(cudaMalloc(&K_, 18 * fb));
             NS3D_CK(cudaMemsetAsync(K_, 0, 18 * fb, s_));
-            NS3D_CK(cudaMalloc(&dpart_, sizeof(double) * 3 * (size_t)NTX * G::NKY * M_));
+            NS3D_CK(cudaMalloc(&dpart_, sizeof(double) * 3 * (size_t)NTXF * G::NKY * M_));
         }
         NS3D_CK(cudaMalloc(&tw_, sizeof(cx<T>) * N));
         NS3D_CK(cudaMalloc(&tab_, sizeof(cx<T>) * (G::KC2 + 1) * M_));
@@ -154,7 +156,7 @@ class Impl final : public Base {
     // ---------------------------------------------------------------- passes
     static constexpr size_t smem_a() { return sizeof(cx<T>) * (size_t)N * TA; }
     static constexpr size_t smem_af() { return sizeof(cx<T>) * (size_t)N * TAF; }
-    static constexpr size_t smem_x() { return sizeof(cx<T>) * (size_t)N * TX; }
+    static constexpr size_t smem_x() { return sizeof(cx<T>) * (size_t)N * TXF; }   // forward x pass
     static constexpr size_t smem_xi() { return xinv_smem<T, N, V>(); }
     static constexpr size_t smem_z() {
         return sizeof(cx<T>) * (size_t)ZP * 3 * zpad<N>() + sizeof(T) * (size_t)ZP * 12 * N;
@@ -209,15 +211,15 @@ class Impl final : public Base {
     }
     template <int INTEG, int MODE>
     void p5x(int m0, int cnt, cx<T>* out) {
-        k_xfwd<T, N, INTEG, MODE, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+        k_xfwd<T, N, INTEG, MODE, V><<<dim3(NTXF, G::NKY, cnt), TXF * PX::P, smem_x(), s_>>>(
             Wm(m0), Um(m0), UTm(m0), out ? out + (size_t)m0 * 3 * G::FS : ACCm(m0), tw_, sdm(m0), tabm(m0),
             (les_ && MODE <= X_STAGE4) ? F_ : nullptr, nullptr, nullptr, RkStage{});
     }
     // RK5-family stage epilogue s (0-based) of members [m0, m0 + cnt)
     void p5tab(int s, int m0, int cnt) {
-        k_xfwd<T, N, INT_TAB, X_STAGE1, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_x(), s_>>>(
+        k_xfwd<T, N, INT_TAB, X_STAGE1, V><<<dim3(NTXF, G::NKY, cnt), TXF * PX::P, smem_x(), s_>>>(
             Wm(m0), Um(m0), UTm(m0), ACCm(m0), tw_, sdm(m0), tabm(m0), les_ ? F_ : nullptr,
-            K_ + (size_t)m0 * 18 * G::FS, dpart_ + (size_t)m0 * 3 * NTX * G::NKY, rk_stage(s, dp5()));
+            K_ + (size_t)m0 * 18 * G::FS, dpart_ + (size_t)m0 * 3 * NTXF * G::NKY, rk_stage(s, dp5()));
     }
     template <int MODE>
     void p5(int m0, int cnt, cx<T>* out = nullptr) {
@@ -243,7 +245,7 @@ class Impl final : public Base {
             k_zpass<T, N, 2><<<(unsigned)((long long)N * N / 2 / ZP), 3 * PA::P * ZP, smem_z(), s_>>>(
                 W_, tw_, tau_real_ + h * 3 * M3, nullptr, 0);
             p4(0, 1);
-            k_xfwd<T, N, INT_IFRK4, X_PLAIN, V><<<dim3(NTX, G::NKY, 1), TX * PX::P, smem_x(), s_>>>(
+            k_xfwd<T, N, INT_IFRK4, X_PLAIN, V><<<dim3(NTXF, G::NKY, 1), TXF * PX::P, smem_x(), s_>>>(
                 W_, U_, UT_, TAU_ + (size_t)h * 3 * G::FS, tw_, sd_, tab_, nullptr, nullptr, nullptr, RkStage{});
         }
         k_sgs_div<T, N><<<kSgsParts, 256, 0, s_>>>(TAU_, U_, F_, sgs_part_);
@@ -302,7 +304,7 @@ class Impl final : public Base {
             p5tab(s, 0, M);
         }
         if (dp) {
-            k_dp_ctl<T, N><<<M, 256, 0, s_>>>(dpart_, NTX * G::NKY, sd_);
+            k_dp_ctl<T, N><<<M, 256, 0, s_>>>(dpart_, NTXF * G::NKY, sd_);
             k_dp_commit<T, N><<<dim3(grid_for((long long)N * N * G::NZP), M), 256, 0, s_>>>(U_, ACC_, sd_);
         }
         k_step_end<T, N><<<M, 256, 0, s_>>>(U_, sd_, p_.forcing == 1 ? p_.force_k : 0, cfl, dp ? 1 : 0);

@@ -74,7 +74,8 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 #ifndef NS3D_TILE_X32
 #define NS3D_TILE_X32 16
 #endif
-// A / AF: pencils per CTA of the inverse / forward y pass; X: of the x passes.
+// A / AF: pencils per CTA of the inverse / forward y pass; X / XF: of the
+// inverse / forward x pass.
 // MINB / MINB_XI: CTAs per SM the x-forward / x-inverse passes are compiled
 // for (registers capped to fit); BATCH: the x-forward epilogue issues all of a
 // thread's state loads of a component before their updates (more registers);
@@ -82,17 +83,20 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 // (two live arrays instead of four; 11 % faster at 256^3, 2 % slower with the
 // 16-element plan of variant 3 at 512^3)
 template <int V> struct TileVar;
-template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<1> { static constexpr int A = 4, AF = 4, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<2> { static constexpr int A = 16, AF = 16, X = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, AF = 16, X = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = false; };
-template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false, STAGE = true; };
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<1> { static constexpr int A = 4, AF = 4, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<2> { static constexpr int A = 16, AF = 16, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, AF = 16, X = 16, XF = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = false; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = 4, XF = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false, STAGE = true; };
+template <> struct TileVar<6> { static constexpr int A = 16, AF = 16, X = 8, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
 
 // Variant 5: the default tiles and plans with the x-forward pass compiled for
 // two CTAs per SM, so one CTA's FFT overlaps another's loads (the x-inverse
 // pass spills too much at 64 registers to gain from the same).
 // Variant 4: 4-pencil x tiles (half-size CTAs, twice as many per SM).
+// Variant 6: variant 2's 16-pencil y tiles and 8-pencil x-inverse tiles with
+// 16-pencil x-forward tiles (the per-kernel best of variants 0 and 2 at 256^3).
 // Plans of variant V: variant 3 gives the x passes a plan with twice the
 // elements per thread (half the threads per pencil), with 16 pencils per CTA
 // (every row access a full 128-byte segment).
@@ -110,9 +114,10 @@ template <typename T, int N, int V = 0, bool INV = true> constexpr int tile_a() 
     return sizeof(T) == 4 ? clip_tile<Plans<N>::A::P, (INV ? TileVar<V>::A : TileVar<V>::AF)>()
                           : (Plans<N>::A::P * 8 <= 512 ? 8 : 4);
 }
-template <typename T, int N, int V = 0> constexpr int tile_x() {
+template <typename T, int N, int V = 0, bool FWD = false> constexpr int tile_x() {
     constexpr int P = PlansV<N, V>::X::P;
-    return sizeof(T) == 4 ? clip_tile<P, TileVar<V>::X>() : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
+    return sizeof(T) == 4 ? clip_tile<P, (FWD ? TileVar<V>::XF : TileVar<V>::X)>()
+                          : (P * 8 <= 256 ? 8 : (P * 4 <= 512 ? 4 : 2));
 }
 // line pairs per CTA of the z pass (>= 96 threads)
 template <int N> constexpr int zpairs() {
@@ -778,14 +783,14 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
 // error partial sums go to dpart[member][block][3] in a fixed order.
 // ---------------------------------------------------------------------------
 template <typename T, int N, int INTEG, int MODE, int V = 0>
-__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, TileVar<V>::MINB)
+__global__ void __launch_bounds__(tile_x<T, N, V, true>() * PlansV<N, V>::X::P, TileVar<V>::MINB)
 k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
        cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tw, const StepDev* __restrict__ sd,
        const cx<T>* __restrict__ tab, const cx<T>* __restrict__ sgs, cx<T>* __restrict__ K,
        double* __restrict__ dpart, const RkStage rs) {
     using G = Geo<N>;
     using PL = typename PlansV<N, V>::X;
-    constexpr int TT = tile_x<T, N, V>();
+    constexpr int TT = tile_x<T, N, V, true>();
     constexpr int E = PL::E, P = PL::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);

@@ -79,6 +79,7 @@ Base* make_f32(int N, const ns3d_params* ps, int M, cudaStream_t s) {
               : v == 3 ? make_f32_v3(N, ps, M, s)
               : v == 4 ? make_f32_v4(N, ps, M, s)
               : v == 5 ? make_f32_v5(N, ps, M, s)
+              : v == 6 ? make_f32_v6(N, ps, M, s)
                        : nullptr;
     if (!b) b = make_f32_v0(N, ps, M, s);
     if (b) b->set_zform(z);

@@ -16,17 +16,17 @@ def run(ns3d, N, steps=5):
 
 @pytest.mark.parametrize("N", [48, 64, 128])
 def test_tile_variants_are_bit_identical(ns3d, N):
-    """Variants 1, 2 and 4 change only the pencils per CTA: bit-identical. Variant 3
+    """Variants 1, 2, 4 and 6 change only the pencils per CTA: bit-identical. Variant 3
     (another x-pass radix plan, where compiled), variant 5 (the per-mode x-forward
     epilogue at two CTAs per SM) and the z-pass forms change the order of
     operations: FP32 rounding."""
     states = {}
-    for v in range(6):
+    for v in range(7):
         for z in (0, 1):
             ns3d.tuning_set(N, v, z)
             states[(v, z)] = run(ns3d, N)
     ns3d.tuning_clear()
-    for v in (1, 2, 4):
+    for v in (1, 2, 4, 6):
         assert np.array_equal(states[(v, 0)], states[(0, 0)])
         assert np.array_equal(states[(v, 1)], states[(0, 1)])
     ref = states[(0, 0)]
@@ -37,7 +37,7 @@ def test_tile_variants_are_bit_identical(ns3d, N):
 def test_autotune_picks_fastest_and_persists(ns3d, tmp_path):
     ns3d.tuning_clear()
     best, tried = ns3d.autotune(64, steps=10, precision="fp32", nu=0.005, dt=1e-3)
-    assert len(tried) == 12   # 6 variants x 2 z-pass forms at 64^3
+    assert len(tried) == 14   # 7 variants x 2 z-pass forms at 64^3
     assert best["ms_per_step"] == min(t["ms_per_step"] for t in tried)
     assert ns3d.tuning(64) == best
     f = tmp_path / "tune.txt"
