@@ -74,7 +74,7 @@ class Impl final : public Base {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
                         (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
-                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_ranges_})
+                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_out_.ranges, (void*)plan_in_.ranges})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -515,10 +515,15 @@ class Impl final : public Base {
     }
     ns3d_status upload(const double* host, cx<T>* dst) {
         if (const void* d = host_dev_ptr(host)) {
-            // the packing kernel reads the dealiased modes straight from the host array
-            k_pack<T, N><<<grid_for((long long)N * N * G::NZP), 256, 0, s_>>>(static_cast<const double2*>(d), dst);
+            // one warp per row's lines reads the dealiased modes straight from the host
+            // array in 512-byte requests; modes outside the sphere are zero in `dst`
+            // (cleared at creation, and no kernel writes them) and stay unwritten
+            ns3d_status st = line_plan(plan_in_, (int)(reinterpret_cast<uintptr_t>(host) & 127));
+            if (st != NS3D_OK) return st;
+            k_pack_lines<T, N><<<(unsigned)((plan_in_.nr * 32LL + 255) / 256), 256, 0, s_>>>(
+                static_cast<const double2*>(d), dst, plan_in_.ranges, plan_in_.nr);
             NS3D_CK(cudaGetLastError());
-            io_h2d_ = sphere_bytes();
+            io_h2d_ = plan_in_.gpu_bytes;
             return NS3D_OK;
         }
         ns3d_status st = ensure_stage();
@@ -531,15 +536,15 @@ class Impl final : public Base {
     }
     ns3d_status download(const cx<T>* src, double* host) {
         if (const void* d = host_dev_ptr(host)) {
-            ns3d_status st = line_plan((int)(reinterpret_cast<uintptr_t>(host) & 127));
+            ns3d_status st = line_plan(plan_out_, (int)(reinterpret_cast<uintptr_t>(host) & 127));
             if (st != NS3D_OK) return st;
-            k_unpack_lines<T, N><<<(unsigned)((plan_nr_ * 32LL + 255) / 256), 256, 0, s_>>>(
-                src, static_cast<double2*>(const_cast<void*>(d)), plan_ranges_, plan_nr_);
+            k_unpack_lines<T, N><<<(unsigned)((plan_out_.nr * 32LL + 255) / 256), 256, 0, s_>>>(
+                src, static_cast<double2*>(const_cast<void*>(d)), plan_out_.ranges, plan_out_.nr);
             NS3D_CK(cudaGetLastError());
             zero_host_lines(reinterpret_cast<unsigned char*>(host));   // host threads, during the GPU work
             NS3D_CK(cudaStreamSynchronize(s_));
             NS3D_CK(cudaGetLastError());
-            io_d2h_ = plan_gpu_bytes_;
+            io_d2h_ = plan_out_.gpu_bytes;
             return NS3D_OK;
         }
         ns3d_status st = ensure_stage();
@@ -550,17 +555,6 @@ class Impl final : public Base {
         NS3D_CK(cudaGetLastError());
         io_d2h_ = kRefBytes;
         return NS3D_OK;
-    }
-    // bytes of the dealiased modes in the reference layout
-    static long long sphere_bytes() {
-        long long n = 0;
-        for (int i = 0; i < N; ++i)
-            for (int j = 0; j < N; ++j) {
-                const int kx = i <= N / 2 ? i : i - N, ky = j <= N / 2 ? j : j - N;
-                const long long rem = (long long)G::KC2 - kx * kx - ky * ky;
-                if (rem >= 0) n += isqrt(rem) + 1;
-            }
-        return 48 * n;
     }
     static long long isqrt(long long v) {
         long long r = (long long)std::sqrt((double)v);
@@ -573,12 +567,18 @@ class Impl final : public Base {
     // with dealiased modes the GPU writes the 128-byte lines that hold them
     // (zeros included where a line extends past them); host threads zero all
     // other bytes. The two sets of lines are disjoint.
-    ns3d_status line_plan(int align) {
-        if (plan_align_ == align) return NS3D_OK;
+    struct LinePlan {
+        int align = -1, nr = 0;
+        long long gpu_bytes = 0;
+        longlong2* ranges = nullptr;                           // [ls, le) in 16-byte units, device
+        std::vector<std::pair<long long, long long>> cpu;      // host-owned byte segments
+    };
+    ns3d_status line_plan(LinePlan& pl, int align) {
+        if (pl.align == align) return NS3D_OK;
         constexpr int NF = N / 2 + 1;
         constexpr long long RB = 48LL * NF;
         std::vector<longlong2> ranges;
-        plan_cpu_.clear();
+        pl.cpu.clear();
         long long cursor = 0, gpu = 0;
         for (long long r = 0; r < (long long)N * N; ++r) {
             const int i = (int)(r / N), j = (int)(r % N);
@@ -590,31 +590,32 @@ class Impl final : public Base {
             if (ls < cursor) ls = cursor;
             if (le > kRefBytes) le = kRefBytes;
             if (ls >= le) continue;
-            if (cursor < ls) plan_cpu_.push_back({cursor, ls - cursor});
+            if (cursor < ls) pl.cpu.push_back({cursor, ls - cursor});
             ranges.push_back(make_longlong2(ls / 16, le / 16));
             gpu += le - ls;
             cursor = le;
         }
-        if (cursor < kRefBytes) plan_cpu_.push_back({cursor, kRefBytes - cursor});
-        if (plan_ranges_) cudaFree(plan_ranges_);
-        plan_ranges_ = nullptr;
-        NS3D_CK(cudaMalloc(&plan_ranges_, sizeof(longlong2) * ranges.size()));
-        NS3D_CK(cudaMemcpy(plan_ranges_, ranges.data(), sizeof(longlong2) * ranges.size(), cudaMemcpyHostToDevice));
-        plan_nr_ = (int)ranges.size();
-        plan_gpu_bytes_ = gpu;
-        plan_align_ = align;
+        if (cursor < kRefBytes) pl.cpu.push_back({cursor, kRefBytes - cursor});
+        if (pl.ranges) cudaFree(pl.ranges);
+        pl.ranges = nullptr;
+        pl.align = -1;
+        NS3D_CK(cudaMalloc(&pl.ranges, sizeof(longlong2) * ranges.size()));
+        NS3D_CK(cudaMemcpy(pl.ranges, ranges.data(), sizeof(longlong2) * ranges.size(), cudaMemcpyHostToDevice));
+        pl.nr = (int)ranges.size();
+        pl.gpu_bytes = gpu;
+        pl.align = align;
         return NS3D_OK;
     }
     // zero the host-owned bytes with up to 16 threads, split evenly by bytes
     void zero_host_lines(unsigned char* host) const {
         long long total = 0;
-        for (const auto& seg : plan_cpu_) total += seg.second;
+        for (const auto& seg : plan_out_.cpu) total += seg.second;
         unsigned nt = std::thread::hardware_concurrency();
         nt = nt < 1 ? 1 : (nt > 16 ? 16 : nt);
         if (total < (1LL << 22)) nt = 1;
         auto work = [&](long long lo, long long hi) {
             long long pos = 0;
-            for (const auto& seg : plan_cpu_) {
+            for (const auto& seg : plan_out_.cpu) {
                 const long long a = pos > lo ? pos : lo, b = pos + seg.second < hi ? pos + seg.second : hi;
                 if (a < b) memset(host + seg.first + (a - pos), 0, (size_t)(b - a));
                 pos += seg.second;
@@ -1002,10 +1003,7 @@ class Impl final : public Base {
     double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]
     // host-array transfers
     long long io_h2d_ = 0, io_d2h_ = 0;
-    int plan_align_ = -1, plan_nr_ = 0;
-    long long plan_gpu_bytes_ = 0;
-    longlong2* plan_ranges_ = nullptr;
-    std::vector<std::pair<long long, long long>> plan_cpu_;
+    LinePlan plan_out_, plan_in_;   // host-array line plans of the download / upload
     int M_ = 1;                    // members
     int m_ = 0;                    // selected member
     std::vector<ns3d_params> mp_;  // per-member parameters

@@ -1519,6 +1519,40 @@ __global__ void k_pack(const double2* __restrict__ ref, cx<T>* __restrict__ U) {
     }
 }
 
+// Host array -> device state for a page-locked host array: one warp per range
+// of 16-byte elements (the 128-byte lines of one (kx, ky) row that hold its
+// dealiased modes), four 512-byte loads in flight per warp; the dealiased modes
+// among them are written to U, the rest of each line is skipped.
+template <typename T, int N>
+__global__ void k_pack_lines(const double2* __restrict__ ref, cx<T>* __restrict__ U,
+                             const longlong2* __restrict__ ranges, int nranges) {
+    using G = Geo<N>;
+    constexpr int NF = N / 2 + 1;
+    const long long w = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (w >= nranges) return;
+    const longlong2 rg = ranges[w];
+    for (long long u0 = rg.x + lane; u0 < rg.y; u0 += 128) {
+        double2 d[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (u0 + 32 * k < rg.y) d[k] = ref[u0 + 32 * k];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const long long u = u0 + 32 * k;
+            if (u >= rg.y) break;
+            const long long e = u / 3;
+            const int c = (int)(u % 3);
+            const long long ij = e / NF;
+            const int kz = (int)(e % NF);
+            const int j = (int)(ij % N), i = (int)(ij / N);
+            const int kx = kof<N>(i), ky = kof<N>(j);
+            if (kz <= G::KC && kx * kx + ky * ky + kz * kz <= G::KC2)
+                U[c * G::FS + ij * G::NZP + kz] = mk(T(d[k].x), T(d[k].y));
+        }
+    }
+}
+
 template <typename T, int N>
 __global__ void k_unpack(const cx<T>* __restrict__ U, double2* __restrict__ ref) {
     using G = Geo<N>;

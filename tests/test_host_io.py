@@ -59,3 +59,25 @@ def test_pinned_alignments_and_in_place(ns3d, offset):
     b.step_host(None, buf)
     a.step_host(None, ref)
     assert np.array_equal(buf, ref)
+
+
+@pytest.mark.parametrize("prec", ["fp64", "fp32"])
+def test_pinned_input_ignores_modes_outside_the_sphere(ns3d, prec):
+    """The pinned upload reads whole 128-byte lines of the host array; values outside
+    the dealiased sphere (NaN here) must not reach the state."""
+    N = 48
+    shape = (N, N, N // 2 + 1, 3)
+    a = ns3d.Solver(N, nu=0.01, dt=1e-3, precision=prec)
+    a.InitialConditions("SPECTRUM", seed=4, k0=3.0)
+    u0 = a.get_state()
+    ref = np.empty(shape, np.complex128)
+    a.step_host(u0, ref)
+    k = np.fft.fftfreq(N, 1.0 / N)
+    kz = np.arange(N // 2 + 1)
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + kz[None, None, :] ** 2
+    buf, keep = pinned_complex(shape)
+    buf[...] = u0
+    buf[k2 > (N // 3) ** 2] = np.nan
+    b = ns3d.Solver(N, nu=0.01, dt=1e-3, precision=prec)
+    b.step_host(buf, buf)
+    assert np.array_equal(buf, ref)
