@@ -407,6 +407,7 @@ def run_les(args, local):
 
     pkg = importlib.import_module("3d_navier_stokes_gb300")
     torch.cuda.set_device(local)
+    pkg.tuning_load(os.path.join(ROOT, "3d_navier_stokes_gb300", "tuning", "gb300.txt"))
     Nf, Nc, nu, dt = 256, 64, 1.5e-3, 1e-3
     dns = pkg.Solver(Nf, nu=nu, dt=dt, precision="fp32", forcing="SHELL", force_k=2, device=local)
     dns.InitialConditions("SPECTRUM", seed=0, k0=3.0)
