@@ -79,17 +79,17 @@ template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = 
 // MINB / MINB_XI: CTAs per SM the x-forward / x-inverse passes are compiled
 // for (registers capped to fit); BATCH: the x-forward epilogue issues all of a
 // thread's state loads of a component before their updates (more registers);
-// STAGE: the x-inverse pass stages two velocity components in shared memory
-// (two live arrays instead of four; 11 % faster at 256^3, 2 % slower with the
-// 16-element plan of variant 3 at 512^3)
+// STAGE: velocity components the x-inverse pass stages in shared memory (2:
+// y and z, two live arrays instead of four, 11 % faster at 256^3; 1: z only,
+// three live arrays, for the 16-element plan of variant 3; 0: none)
 template <int V> struct TileVar;
-template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<1> { static constexpr int A = 4, AF = 4, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<2> { static constexpr int A = 16, AF = 16, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, AF = 16, X = 16, XF = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = false; };
-template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = 4, XF = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
-template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false, STAGE = true; };
-template <> struct TileVar<6> { static constexpr int A = 16, AF = 16, X = 8, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true, STAGE = true; };
+template <> struct TileVar<0> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 2; };
+template <> struct TileVar<1> { static constexpr int A = 4, AF = 4, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 2; };
+template <> struct TileVar<2> { static constexpr int A = 16, AF = 16, X = 8, XF = 8, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 2; };
+template <> struct TileVar<3> { static constexpr int A = NS3D_TILE_A32, AF = 16, X = 16, XF = 16, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 1; };
+template <> struct TileVar<4> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = 4, XF = 4, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 2; };
+template <> struct TileVar<5> { static constexpr int A = NS3D_TILE_A32, AF = NS3D_TILE_A32, X = NS3D_TILE_X32, XF = NS3D_TILE_X32, MINB = 2, MINB_XI = 1; static constexpr bool BATCH = false; static constexpr int STAGE = 2; };
+template <> struct TileVar<6> { static constexpr int A = 16, AF = 16, X = 8, XF = NS3D_TILE_X32, MINB = 1, MINB_XI = 1; static constexpr bool BATCH = true; static constexpr int STAGE = 2; };
 
 // Variant 5: the default tiles and plans with the x-forward pass compiled for
 // two CTAs per SM, so one CTA's FFT overlaps another's loads (the x-inverse
@@ -203,7 +203,7 @@ enum { X_STAGE1 = 0, X_STAGE2 = 1, X_STAGE3 = 2, X_STAGE4 = 3, X_RHS = 8, X_PLAI
 // ---------------------------------------------------------------------------
 template <typename T, int N, int V = 0>
 constexpr size_t xinv_smem() {
-    return sizeof(cx<T>) * (size_t)N * tile_x<T, N, V>() * (TileVar<V>::STAGE ? 3 : 1);
+    return sizeof(cx<T>) * (size_t)N * tile_x<T, N, V>() * (1 + TileVar<V>::STAGE);
 }
 template <typename T, int N, int V = 0>
 __global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, TileVar<V>::MINB_XI)
@@ -233,20 +233,21 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     StridedIdx<TT, PL::R1> sidx{t};
     SyncBlock sync;
 
-    constexpr bool kStage = TileVar<V>::STAGE;
-    // components 1 and 2: asynchronous copies, zero-filled outside the sphere
+    constexpr int kStage = TileVar<V>::STAGE;
+    constexpr int kC0 = 3 - kStage;   // first staged component
+    // the staged components: asynchronous copies, zero-filled outside the sphere
 #pragma unroll
-    for (int c = 1; c <= (kStage ? 2 : 0); ++c) {
+    for (int c = kC0; c <= 2; ++c) {
         const cx<T>* src = U + (long long)c * G::FS + off;
 #pragma unroll
         for (int s = 0; s < E; ++s) {
             const int kx = kof<N>(p + P * s);
             const bool in = colok && kx * kx <= rem;
-            cp_async<sizeof(cx<T>)>(&stg[((c - 1) * E + s) * NT + threadIdx.x],
+            cp_async<sizeof(cx<T>)>(&stg[((c - kC0) * E + s) * NT + threadIdx.x],
                                     in ? src + (long long)(p + P * s) * xs : U, in ? (uint32_t)sizeof(cx<T>) : 0u);
         }
     }
-    if (kStage) cp_async_commit();
+    if (kStage > 0) cp_async_commit();
     auto load = [&](int c, cx<T>(&v)[E]) {
         const cx<T>* src = U + (long long)c * G::FS + off;
 #pragma unroll
@@ -258,7 +259,7 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     auto staged = [&](int c, cx<T>(&v)[E]) {
         cp_async_wait_all();
 #pragma unroll
-        for (int s = 0; s < E; ++s) v[s] = stg[((c - 1) * E + s) * NT + threadIdx.x] * scale;
+        for (int s = 0; s < E; ++s) v[s] = stg[((c - kC0) * E + s) * NT + threadIdx.x] * scale;
     };
     auto ikx = [&](const cx<T>(&v)[E], cx<T>(&o)[E]) {
 #pragma unroll
@@ -272,7 +273,38 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     };
 
     const T fky = T(ky), fkz = T(kz);
-    if constexpr (!kStage) {
+    if constexpr (kStage == 1) {
+        // x and y components in registers, z staged: three live arrays
+        cx<T> X[E], Y[E], B[E];
+        load(0, X);
+        load(1, Y);
+        ikx(Y, B);
+        PL::inv(B, sbuf, p, tw, sidx, sync);
+        PL::inv(X, sbuf, p, tw, sidx, sync);
+        store(0, X);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = B[s] - mul_i(X[s]) * fky;
+        store(5, B);
+        {
+            cx<T> Z[E];
+            staged(2, Z);
+            ikx(Z, B);
+        }
+        PL::inv(B, sbuf, p, tw, sidx, sync);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = mul_i(X[s]) * fkz - B[s];
+        store(4, B);
+        PL::inv(Y, sbuf, p, tw, sidx, sync);
+        store(1, Y);
+        staged(2, X);   // uz
+        PL::inv(X, sbuf, p, tw, sidx, sync);
+        store(2, X);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = mul_i(X[s]) * fky - mul_i(Y[s]) * fkz;
+        store(3, B);
+        return;
+    }
+    if constexpr (kStage == 0) {
         // every component in registers up front
         cx<T> X[E], Y[E], Z[E], B[E];
         load(0, X);
@@ -868,7 +900,7 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
         // then, in chunks of up to 8 modes and per component, the chunk's state
         // loads before their updates, so that a chunk's loads (per array) are in
         // flight at once
-        constexpr int CH = E > 8 ? 8 : E;
+        constexpr int CH = E > 8 ? 4 : E;
         unsigned valid = 0u;
         int k2s[E];
 #pragma unroll
