@@ -94,6 +94,8 @@ Base* make_f32_v2(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v3(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v4(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v5(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f32_v3_large(int N, const ns3d_params* ps, int M, cudaStream_t s);
+Base* make_f64_large(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v6(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f64_v0(int N, const ns3d_params* ps, int M, cudaStream_t s);
 bool supported_n(int N);

@@ -1,6 +1,6 @@
 // ns3d_inst_f32_v3.cu — FP32-bulk engines in variant 3 (x passes with twice
 // the elements per thread and 16-pencil tiles, PlansV<N, 3>) for the sizes
-// where that plan exists.
+// where that plan exists (1024^3 in ns3d_inst_f32_v3_large.cu).
 #include "ns3d_inst.cuh"
 
 namespace ns3d {

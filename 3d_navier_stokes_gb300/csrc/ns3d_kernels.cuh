@@ -105,6 +105,7 @@ template <> struct AltX<64> { using X = Plan<64, 16, 16, 4>; };
 template <> struct AltX<128> { using X = Plan<128, 16, 16, 8>; };
 template <> struct AltX<256> { using X = Plan<256, 16, 16, 16>; };
 template <> struct AltX<512> { using X = Plan<512, 16, 8, 8, 8>; };
+template <> struct AltX<1024> { using X = Plan<1024, 16, 8, 8, 4, 4>; };
 template <int N, int V> struct PlansV {
     using A = typename Plans<N>::A;
     using X = typename std::conditional<(V == 3), typename AltX<N>::X, typename Plans<N>::X>::type;

@@ -76,7 +76,7 @@ Base* make_f32(int N, const ns3d_params* ps, int M, cudaStream_t s) {
     shape_for(N, NS3D_FP32, &v, &z);
     Base* b = v == 1   ? make_f32_v1(N, ps, M, s)
               : v == 2 ? make_f32_v2(N, ps, M, s)
-              : v == 3 ? make_f32_v3(N, ps, M, s)
+              : v == 3 ? (N >= 1024 ? make_f32_v3_large(N, ps, M, s) : make_f32_v3(N, ps, M, s))
               : v == 4 ? make_f32_v4(N, ps, M, s)
               : v == 5 ? make_f32_v5(N, ps, M, s)
               : v == 6 ? make_f32_v6(N, ps, M, s)
