@@ -643,10 +643,10 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
     using G = Geo<N>;
     using PL = typename ZPlan<N>::A;
     constexpr int E = PL::E, P = PL::P, GPW = zline_gpw<N>(), GW = zline_gw<N>(), GT = 32 * GW;
-    // FP32x2 butterfly additions where one line fills one warp (512 points; 4 %
-    // faster there); the 256-point lines of two per warp need the registers for
-    // three CTAs per SM, and the two-warp lines of 1024 points keep the scalar form
-    constexpr bool kPK = GPW == 1 && GW == 1;
+    // FP32x2 butterfly additions where a line fills one warp or more (512 points:
+    // 4 % faster; 1024 points: 2.6 %); the 256-point lines of two per warp need
+    // the registers for three CTAs per SM
+    constexpr bool kPK = GPW == 1;
     constexpr int NGRP = zline_groups<N>();
     constexpr int NZP = G::NZP;
     constexpr long long NG = (long long)N * N / GPW;   // work items (line groups) per ensemble member
