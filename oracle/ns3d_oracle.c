@@ -4,16 +4,21 @@
  * CPU FP64 restatement of the reference solver's time-stepping hot path
  * (Solver/src/solver.c). Used by tests/ as the parity checker and by bench.py
  * as the timed CPU baseline. Each function cites the reference lines it
- * restates. The reference itself cannot be compiled here: it needs FFTW3-MPI,
- * MPI and parallel HDF5, none of which exist on either machine.
+ * restates. The reference program needs FFTW3-MPI, MPI and parallel HDF5,
+ * none of which exist on either machine; its hot-path sources solver.c and
+ * utils.c do compile unchanged against the single-rank stand-ins of
+ * oracle/ref_shim (make -C oracle ref -> oracle/_ref).
  *
- * Parity pinning: the reference ships no golden vectors. This restatement is
- * pinned by (1) its FFT against numpy.fft (pocketfft) and a direct DFT, the
- * stand-in for the reference's FFTW calls (solver.c:656,658,683,1573,1599);
- * (2) the reference's own known-answer test, the Shapiro exact solution
- * (solver.c:1654-1702), and the Taylor–Green invariants E = pi^3,
- * Omega = 3 pi^3 at t = 0; (3) an independent numpy restatement of the RHS
- * and both integrators (tests/golden/make_golden.py).
+ * Parity pinning: (1) the reference's own code: with the bug-compatibility
+ * flags below, this restatement agrees with solver.c's NonlinearRHSBatch,
+ * RK4Step, ApplyDealiasing, ComputeSystemMeasurables, InitialConditions and
+ * the SpectralSolve loop (tests/test_reference_parity.py, and fixtures made
+ * from it, tests/golden/ref_N16.npz); (2) its FFT against numpy.fft
+ * (pocketfft) and a direct DFT, the stand-in for the reference's FFTW calls
+ * (solver.c:656,658,683,1573,1599); (3) the reference's known-answer test,
+ * the Shapiro exact solution (solver.c:1654-1702), and the Taylor–Green
+ * invariants E = pi^3, Omega = 3 pi^3 at t = 0; (4) an independent numpy
+ * restatement of the RHS and the integrators (tests/golden/make_golden.py).
  *
  * Defects of the reference (solver.c) are fixed here, each behind a flag where
  * reproducing it is meaningful:
@@ -153,6 +158,27 @@ void orc_fft1d(int n, const double* in, double* out, int inverse) {
     plan_init(&p, n);
     fft_exec(&p, (const cplx*)in, (cplx*)out, inverse);
     plan_free(&p);
+}
+
+/* Planned form of orc_fft1d, for callers that transform many lines of one
+   length (the single-rank FFTW-MPI stand-in under oracle/ref_shim). */
+struct orc_fft_plan_s { fft_plan p; };
+
+orc_fft_plan_t* orc_fft_plan_create(int n) {
+    if (n < 1) return NULL;
+    orc_fft_plan_t* q = (orc_fft_plan_t*)malloc(sizeof(orc_fft_plan_t));
+    plan_init(&q->p, n);
+    return q;
+}
+
+void orc_fft_plan_exec(const orc_fft_plan_t* q, const double* in, double* out, int inverse) {
+    fft_exec(&q->p, (const cplx*)in, (cplx*)out, inverse);
+}
+
+void orc_fft_plan_destroy(orc_fft_plan_t* q) {
+    if (!q) return;
+    plan_free(&q->p);
+    free(q);
 }
 
 /* ------------------------------------------------------------------------ */

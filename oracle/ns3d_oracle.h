@@ -57,6 +57,11 @@ void   orc_set_forcing_target(orc_ctx* c, double e);
 void orc_fft_r2c(orc_ctx* c, const double* real, double* u_hat);
 void orc_fft_c2r(orc_ctx* c, const double* u_hat, double* real);
 void orc_fft1d(int n, const double* in, double* out, int inverse);
+/* planned 1D complex transform of length n (in != out, contiguous), unnormalised */
+typedef struct orc_fft_plan_s orc_fft_plan_t;
+orc_fft_plan_t* orc_fft_plan_create(int n);
+void orc_fft_plan_exec(const orc_fft_plan_t* q, const double* in, double* out, int inverse);
+void orc_fft_plan_destroy(orc_fft_plan_t* q);
 
 void orc_dealias(orc_ctx* c, double* arr, int array_dim);
 void orc_rhs(orc_ctx* c, const double* u_hat, double* rhs);

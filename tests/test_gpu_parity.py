@@ -247,3 +247,17 @@ def test_fp32_512_tracks_fp64(ns3d):
     e32, k32 = res["fp32"]
     assert abs(e32 - e64) < 1e-6 * e64
     assert np.max(np.abs(k32 - k64)) < 1e-6 * k64.max()
+
+
+def test_spectra_match_reference_fixture(ns3d):
+    """E(k), Omega(k) and the energy and enstrophy of the FP64 GPU path against
+    the reference's own ComputeSystemMeasurables output (tests/golden/ref_N16.npz;
+    its spectra carry none of the reference's defects)."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_N16.npz"))
+    s = ns3d.Solver(16, nu=0.01, precision="fp64")
+    s.set_state(d["uh"])
+    tot, Ek, Ok = s.ComputeSystemMeasurables()
+    assert rel_l2(Ek, d["Ek"]) < FP64_TOL and rel_l2(Ok, d["Ok"]) < FP64_TOL
+    assert abs(tot["energy"] - d["Ek"].sum()) <= FP64_TOL * tot["energy"]
+    assert abs(tot["enstrophy"] - d["Ok"].sum()) <= FP64_TOL * tot["enstrophy"]
