@@ -46,6 +46,7 @@ EXPORTS = (
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
+    "ns3d_set_wait_budget",
     "ns3d_les_infer_host", "ns3d_les_profile_infer", "ns3d_io_bytes",
     "ns3d_autotune", "ns3d_autotune_ensemble", "ns3d_tuning_get", "ns3d_tuning_set", "ns3d_tuning_clear", "ns3d_tuning_save",
     "ns3d_tuning_load", "ns3d_increment_stats",
@@ -156,6 +157,8 @@ def lib():
         L.ns3d_set_dp_tolerances.restype = I
         L.ns3d_set_dp_tolerances.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.ns3d_dp_stats.restype = I
+        L.ns3d_set_wait_budget.restype = I
+        L.ns3d_set_wait_budget.argtypes = [P, ctypes.c_longlong]
         L.ns3d_dp_stats.argtypes = [P, D, ctypes.POINTER(ctypes.c_long)]
         L.ns3d_autotune.restype = I
         L.ns3d_autotune.argtypes = [ctypes.POINTER(Params), I, ctypes.POINTER(Tuning), ctypes.POINTER(Tuning), I,
@@ -481,6 +484,11 @@ class Solver:
     def set_dp_tolerances(self, atol: float, rtol: float):
         """DP5CN error tolerances (DP_ABS_TOL, DP_REL_TOL; default 1e-7 each)."""
         self._ck(lib().ns3d_set_dp_tolerances(self._h, atol, rtol))
+
+    def set_wait_budget(self, cycles: int):
+        """Clock-cycle budget of the z pass's bounded waits (<= 0: the
+        default); a step whose wait runs out raises with ERR_TIMEOUT."""
+        self._ck(lib().ns3d_set_wait_budget(self._h, int(cycles)))
 
     def dp_stats(self):
         """(error norm of the last DP5CN attempt, rejected attempts so far)"""

@@ -281,6 +281,11 @@ ns3d_status ns3d_io_bytes(ns3d_ctx* c, long long* h2d, long long* d2h) {
     return pass(c, c->impl->io_bytes(h2d, d2h));
 }
 
+ns3d_status ns3d_set_wait_budget(ns3d_ctx* c, long long cycles) {
+    if (!c) return NS3D_ERR_INVALID;
+    return pass(c, c->impl->set_wait_budget(cycles));
+}
+
 ns3d_status ns3d_dp_stats(ns3d_ctx* c, double* last_err, long* rejects) {
     if (!c) return NS3D_ERR_INVALID;
     return pass(c, c->impl->dp_stats(last_err, rejects));

@@ -45,6 +45,8 @@ class Base {
     virtual ns3d_status set_forcing_target(double e) = 0;
     virtual ns3d_status set_dp_tolerances(double atol, double rtol) = 0;
     virtual ns3d_status dp_stats(double* err, long* rejects) = 0;
+    // clock-cycle budget of the z pass's bounded waits (<= 0: the default)
+    virtual ns3d_status set_wait_budget(long long cycles) = 0;
     virtual ns3d_status io_bytes(long long* h2d, long long* d2h) = 0;
     virtual ns3d_status increment_stats(const int* incr, int nr, int nbins, double* stats, double* ranges,
                                         double* counts) = 0;

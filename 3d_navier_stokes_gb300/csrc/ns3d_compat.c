@@ -33,9 +33,13 @@ static ns3d_params params_from_sys(double dt) {
     p.nu = sys_vars->NU;
     p.dt = dt > 0 ? dt : sys_vars->dt;
     p.t0 = sys_vars->t0;
-    p.visc_pow = sys_vars->hyper_visc ? 2 : 1;
-    p.integrator = (sys_vars->integrator >= NS3D_RK4CN && sys_vars->integrator <= NS3D_DP5CN) ? sys_vars->integrator
-                                                                                             : NS3D_IFRK4;
+    /* zero-filled switches select the reference's default build: nu k^4 and
+       RK4 + Crank-Nicolson (Makefile:44, data_types.h:57-71) */
+    p.visc_pow = sys_vars->visc_pow == 1 ? 1 : 2;
+    p.integrator = sys_vars->integrator == 1   ? NS3D_IFRK4
+                   : sys_vars->integrator == 2 ? NS3D_RK5CN
+                   : sys_vars->integrator == 3 ? NS3D_DP5CN
+                                               : NS3D_RK4CN;
     p.precision = sys_vars->precision == 1 ? NS3D_FP32 : NS3D_FP64;
     p.cfl = (sys_vars->adaptive_step && p.integrator != NS3D_DP5CN) ? sys_vars->CFL_CONST : 0.0;
     p.forcing = strcmp(sys_vars->forcing, "SHELL") == 0 ? NS3D_FORCE_SHELL : NS3D_FORCE_NONE;
@@ -133,7 +137,7 @@ void RK5DPStep(const double dt, const long int* N, const int iters, const ptrdif
     (void)iters;
     (void)local_Nx;
     (void)RK_data;
-    if (!sys_vars || (sys_vars->integrator != NS3D_RK5CN && sys_vars->integrator != NS3D_DP5CN)) {
+    if (!sys_vars || (sys_vars->integrator != 2 && sys_vars->integrator != 3)) {
         fprintf(stderr, "\n[ERROR] --- RK5DPStep needs sys_vars->integrator 2 (RK5) or 3 (DPRK5)\n-->> Exiting!!!\n");
         exit(1);
     }
@@ -141,10 +145,10 @@ void RK5DPStep(const double dt, const long int* N, const int iters, const ptrdif
     double t = 0, cur_dt = 0;
     long it = 0;
     ns3d_status s = ns3d_get_time(c, &t, &cur_dt, &it);
-    if (s == NS3D_OK && sys_vars->integrator == NS3D_RK5CN && cur_dt != dt && !sys_vars->adaptive_step)
+    if (s == NS3D_OK && sys_vars->integrator == 2 && cur_dt != dt && !sys_vars->adaptive_step)
         s = ns3d_set_time(c, t, dt, it);
     if (s == NS3D_OK) s = ns3d_step_host(c, (const double*)run_data->u_hat, (double*)run_data->u_hat);
-    if (s == NS3D_OK && sys_vars->integrator == NS3D_DP5CN) {
+    if (s == NS3D_OK && sys_vars->integrator == 3) {
         s = ns3d_get_time(c, &t, &cur_dt, &it);
         sys_vars->dt = cur_dt;
         sys_vars->t = t;

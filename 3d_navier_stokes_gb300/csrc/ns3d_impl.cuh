@@ -125,6 +125,7 @@ class Impl final : public Base {
             StepDev sd{};
             sd.t = mp_[m].t0; sd.dt = mp_[m].dt; sd.t0 = mp_[m].t0; sd.nu = mp_[m].nu; sd.cfl = mp_[m].cfl;
             sd.dp_atol = 1e-7; sd.dp_rtol = 1e-7;   // DP_ABS_TOL, DP_REL_TOL (data_types.h:123-124)
+            sd.wait_cycles = kWaitCycles;
             sd_host_[m] = sd;
         }
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
@@ -887,6 +888,14 @@ class Impl final : public Base {
             sd_host_[m].dp_atol = atol;
             sd_host_[m].dp_rtol = rtol;
         }
+        NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        return NS3D_OK;
+    }
+    ns3d_status set_wait_budget(long long cycles) override {
+        NS3D_CK(cudaMemcpyAsync(sd_host_, sd_, sizeof(StepDev) * M_, cudaMemcpyDeviceToHost, s_));
+        NS3D_CK(cudaStreamSynchronize(s_));
+        for (int m = 0; m < M_; ++m) sd_host_[m].wait_cycles = cycles > 0 ? cycles : kWaitCycles;
         NS3D_CK(cudaMemcpyAsync(sd_, sd_host_, sizeof(StepDev) * M_, cudaMemcpyHostToDevice, s_));
         NS3D_CK(cudaStreamSynchronize(s_));
         return NS3D_OK;

@@ -160,6 +160,7 @@ struct StepDev {
     unsigned long long umax_bits;    // running max of the stage-1 z pass (bits of T, non-negative)
     long long iters;
     int status;                      // 0 ok; 5 numeric
+    long long wait_cycles;           // budget of the z pass's first wait on each copy (kWaitCycles by default)
     int sgs_on;                      // learned closure used in this step (energy-budget check passed)
     long long sgs_steps, sgs_fallbacks;
     // Dormand-Prince step control (DP5CN)
@@ -700,12 +701,14 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         um = T(0);
     };
     int s = 0;
+    const long long budget = sd[0].wait_cycles > 0 ? sd[0].wait_cycles : kWaitCycles;
     if (g < NGT) issue(g, 0);
     for (; g < NGT; g += nw, s ^= 1) {
         const bool more = g + nw < NGT;
         if (more) issue(g + nw, s ^ 1);
         // every thread waits (bounded) for the copies; the group agrees on the outcome
-        bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], (phase >> s) & 1u));
+        const uint32_t par = (phase >> s) & 1u;
+        bool ok = __all_sync(0xffffffffu, mbar_wait(&bars[s], par, budget));
         if constexpr (GW > 1) {
             if (lane == 0) votes[gt >> 5] = ok ? 1 : 0;
             sync();
@@ -715,8 +718,10 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
         }
         phase ^= 1u << s;
         if (!ok) {
-            // record the timeout, let the copy already issued for the next group land, leave
-            if (more) (void)mbar_wait(&bars[s ^ 1], (phase >> (s ^ 1)) & 1u);
+            // record the timeout; let the copies of both stages still in flight
+            // land (full budget) before the CTA and its shared memory go away
+            (void)mbar_wait(&bars[s], par, kWaitCycles);
+            if (more) (void)mbar_wait(&bars[s ^ 1], (phase >> (s ^ 1)) & 1u, kWaitCycles);
             if (gt == 0) atomicExch(&sd[g / NG].status, kStatusTimeout);
             return;
         }
@@ -1277,9 +1282,13 @@ __global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int 
     U += (long long)blockIdx.x * 3 * G::FS;   // one CTA per ensemble member
     sd += blockIdx.x;
     __shared__ double red[256];
-    // a rejected DP5CN attempt leaves the state, the time and the forcing alone
+    // a rejected DP5CN attempt leaves the state, the time and the forcing alone.
+    // The energy of the shells round(|k|) <= kb is summed every step: it is the
+    // forcing's measure, and without forcing (kb = 1) the numeric health check
+    // (a NaN or Inf anywhere in the field reaches these shells through the
+    // nonlinear term within one step)
     const bool rejected = dp && !sd->dp_accept;
-    const int kb = rejected ? 0 : force_k;
+    const int kb = rejected ? 0 : (force_k > 0 ? force_k : 1);
     const int side = 2 * kb + 1;
     const int nbox = side * side * (kb + 1);
     const long long k2max = (long long)kb * (kb + 1);
@@ -1307,7 +1316,7 @@ __global__ void k_step_end(cx<T>* __restrict__ U, StepDev* __restrict__ sd, int 
     }
     const double en = red[0] * 8.0 * 3.14159265358979323846 * 3.14159265358979323846 * 3.14159265358979323846 * 0.5 /
                       ((double)N * N * N * (double)N * N * N);
-    if (kb > 0 && en > 0.0 && sd->force_target > 0.0) {
+    if (force_k > 0 && kb > 0 && en > 0.0 && sd->force_target > 0.0) {
         const T sc = T(sqrt(sd->force_target / en));
         for (int q = threadIdx.x; q < nbox; q += blockDim.x) {
             const int kx = q % side - kb, ky = (q / side) % side - kb, kz = q / (side * side);

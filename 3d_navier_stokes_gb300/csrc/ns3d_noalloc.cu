@@ -10,6 +10,13 @@
 // ns3d_measurables keeps in a context allocation live here in a file-scope
 // static __device__ array of fixed size instead.
 //
+// What it computes: every mode of the caller's array counts, with the
+// reference's multiplicities (1 on the kz = 0 and kz = N/2 planes, 2
+// elsewhere, solver.c:1230-1262); shells with round(|k|) >= n_spect (corner
+// modes outside the 2/3 sphere, for N whose sqrt(3)N/2 has a fraction >= 1/2)
+// are left out of E(k) and Omega(k) but stay in the totals: the reference
+// writes one element past its spectrum arrays there (solver.c:1242-1250).
+//
 // Limits and sharing:
 //   * N <= 512 (the partials of a 512^3 grid fill at most 228,608 of the
 //     262,144 doubles = 2 MiB of the array); larger N is rejected.
@@ -19,10 +26,15 @@
 //     writes every slot it later reads, so nothing has to be cleared, but two
 //     calls whose kernels overlap on the GPU (different streams, or different
 //     host threads) race on the array and corrupt each other's results.
-//   * The first call on a device, with that device current, looks up the
-//     array's device address (cudaGetSymbolAddress); make that first call
-//     before any stream capture begins.
+//   * Outside stream capture each call looks up the array's device address
+//     for the current context (cudaGetSymbolAddress) and remembers it under
+//     that context's unique id. A call made while its stream is being
+//     captured uses the remembered address of the current context, so the
+//     first call in a context (and the first after a cudaDeviceReset, which
+//     makes a new context) must come before any stream capture; otherwise it
+//     returns NS3D_ERR_INVALID.
 #include <mutex>
+#include <stdint.h>
 #include <stdio.h>
 
 #include "../../include/ns3d.h"
@@ -149,14 +161,82 @@ __global__ void k_reduce_out(const double* __restrict__ part, int nparts, int ns
 }
 
 std::mutex g_mu;
-constexpr int kMaxDevices = 64;
-double* g_addr[kMaxDevices] = {};
+constexpr int kMaxContexts = 64;
+struct ScratchEntry {
+    unsigned long long ctx_id;
+    double* addr;
+};
+ScratchEntry g_cache[kMaxContexts];
+int g_cached = 0;
+
+typedef int (*ctx_get_current_fn)(void**);
+typedef int (*ctx_get_id_fn)(void*, unsigned long long*);
+
+// The driver's unique id of the calling thread's current context (ids are
+// never reused within a process), through the runtime's driver entry points.
+bool current_context_id(unsigned long long* id) {
+    static ctx_get_current_fn get_current = nullptr;
+    static ctx_get_id_fn get_id = nullptr;
+    if (!get_current || !get_id) {
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        cudaDriverEntryPointQueryResult q1, q2;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q2 != cudaDriverEntryPointSuccess)
+            return false;
+        get_current = reinterpret_cast<ctx_get_current_fn>(f1);
+        get_id = reinterpret_cast<ctx_get_id_fn>(f2);
+    }
+    void* ctx = nullptr;
+    if (get_current(&ctx) != 0 || !ctx) return false;
+    return get_id(ctx, id) == 0;
+}
+
+// The device address of g_scratch in the current context (see the file
+// comment for when it is looked up and when a remembered one is used).
+ns3d_status scratch_address(cudaStream_t s, double** out) {
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return NS3D_ERR_CUDA;
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (cap == cudaStreamCaptureStatusNone) {
+        void* p = nullptr;
+        unsigned long long id = 0;
+        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return NS3D_ERR_CUDA;
+        if (!current_context_id(&id)) return NS3D_ERR_CUDA;
+        int slot = -1;
+        for (int q = 0; q < g_cached; ++q)
+            if (g_cache[q].ctx_id == id) slot = q;
+        if (slot < 0) {
+            slot = g_cached < kMaxContexts ? g_cached++ : (int)(id % kMaxContexts);
+            g_cache[slot].ctx_id = id;
+        }
+        g_cache[slot].addr = static_cast<double*>(p);
+        *out = static_cast<double*>(p);
+        return NS3D_OK;
+    }
+    unsigned long long id = 0;
+    if (!current_context_id(&id)) return NS3D_ERR_CUDA;
+    for (int q = 0; q < g_cached; ++q)
+        if (g_cache[q].ctx_id == id) {
+            *out = g_cache[q].addr;
+            return NS3D_OK;
+        }
+    fprintf(stderr, "ns3d_measurables_noalloc: first call in this context made during stream capture; "
+                    "make one call before capturing\n");
+    return NS3D_ERR_INVALID;
+}
 
 }  // namespace
 
 extern "C" ns3d_status ns3d_measurables_noalloc(int N, double nu, int visc_pow, const double* d_u_hat,
                                                 double* d_totals, double* d_Ek, double* d_Ok, void* stream) {
     if (N <= 2 || (N % 2) != 0 || !d_u_hat || !d_totals || (visc_pow != 1 && visc_pow != 2)) return NS3D_ERR_INVALID;
+    // the state is read as 16-byte complex pairs, the outputs as doubles
+    if ((reinterpret_cast<uintptr_t>(d_u_hat) & 15) != 0 || (reinterpret_cast<uintptr_t>(d_totals) & 7) != 0 ||
+        (reinterpret_cast<uintptr_t>(d_Ek) & 7) != 0 || (reinterpret_cast<uintptr_t>(d_Ok) & 7) != 0)
+        return NS3D_ERR_INVALID;
     const int nsp = ns3d_n_spect(N);
     const long long nparts = ((long long)N * N + kLinesPerCta - 1) / kLinesPerCta;
     const long long need = nparts * (5 + 2 * (long long)nsp);
@@ -166,24 +246,25 @@ extern "C" ns3d_status ns3d_measurables_noalloc(int N, double nu, int visc_pow, 
                 N, need, kScratchDoubles, kMaxN);
         return NS3D_ERR_INVALID;
     }
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return NS3D_ERR_CUDA;
-    double* scratch = nullptr;
-    {
-        std::lock_guard<std::mutex> lk(g_mu);
-        if (!g_addr[dev]) {
-            void* p = nullptr;
-            if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return NS3D_ERR_CUDA;
-            g_addr[dev] = static_cast<double*>(p);
-        }
-        scratch = g_addr[dev];
-    }
     cudaStream_t s = static_cast<cudaStream_t>(stream);
+    double* scratch = nullptr;
+    const ns3d_status st = scratch_address(s, &scratch);
+    if (st != NS3D_OK) return st;
+    // each launch's own status: an earlier error of the caller's program is
+    // neither reported as ours nor cleared
     const size_t smem = sizeof(double) * ((size_t)kWarps * 2 * nsp + (size_t)kWarps * 5);
-    k_measure_ref<<<(unsigned)nparts, kWarps * 32, smem, s>>>(reinterpret_cast<const double2*>(d_u_hat), N, nu,
-                                                             visc_pow, nsp, scratch);
+    const double2* u = reinterpret_cast<const double2*>(d_u_hat);
+    void* a1[] = {(void*)&u, (void*)&N, (void*)&nu, (void*)&visc_pow, (void*)&nsp, (void*)&scratch};
+    if (cudaLaunchKernel((const void*)k_measure_ref, dim3((unsigned)nparts), dim3(kWarps * 32), a1, smem, s) !=
+        cudaSuccess)
+        return NS3D_ERR_CUDA;
     const double N3 = (double)N * N * N;
+    const double N3sq = N3 * N3;
     const int width = 5 + 2 * nsp;
-    k_reduce_out<<<(width + 127) / 128, 128, 0, s>>>(scratch, (int)nparts, nsp, N3 * N3, d_totals, d_Ek, d_Ok);
-    return cudaGetLastError() == cudaSuccess ? NS3D_OK : NS3D_ERR_CUDA;
+    const int np = (int)nparts;
+    const double* part = scratch;
+    void* a2[] = {(void*)&part, (void*)&np, (void*)&nsp, (void*)&N3sq, (void*)&d_totals, (void*)&d_Ek, (void*)&d_Ok};
+    if (cudaLaunchKernel((const void*)k_reduce_out, dim3((width + 127) / 128), dim3(128), a2, 0, s) != cudaSuccess)
+        return NS3D_ERR_CUDA;
+    return NS3D_OK;
 }

@@ -2,9 +2,11 @@
 // (cp.async.bulk / cp.async.bulk.tensor) completed through shared-memory
 // mbarriers, with bounded waits.
 //
-// Every wait gives up after kWaitCycles SM clock cycles (about 2 s at 2 GHz);
-// the caller then records NS3D_ERR_TIMEOUT in the step status word and
-// returns instead of spinning forever.
+// Every wait gives up after a budget of SM clock cycles (kWaitCycles, about
+// 2 s at 2 GHz, unless the caller passes a shorter one); the caller then
+// records NS3D_ERR_TIMEOUT in the step status word and returns instead of
+// spinning forever. Waits that drain copies still in flight before a CTA
+// exits always use the full kWaitCycles.
 #pragma once
 #include <cuda.h>
 #include <cuda_runtime.h>
@@ -85,12 +87,34 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
     return ok != 0;
 }
 
+// non-blocking test of phase `parity`
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// budgets below this are checked with non-blocking tests only: try_wait may
+// suspend the thread for a hardware-defined time, longer than such a budget
+constexpr long long kShortBudget = 100000;
+
 // bounded wait on phase `parity`; false on timeout
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, long long budget = kWaitCycles) {
+    if (budget < kShortBudget) {
+        const long long t0 = clock64();
+        do {
+            if (mbar_test_wait(bar, parity)) return true;
+        } while (clock64() - t0 <= budget);
+        return false;
+    }
     if (mbar_try_wait(bar, parity)) return true;
     const long long t0 = clock64();
     while (!mbar_try_wait(bar, parity)) {
-        if (clock64() - t0 > kWaitCycles) return false;
+        if (clock64() - t0 > budget) return false;
     }
     return true;
 }

@@ -39,7 +39,8 @@ typedef struct {
 
 static void usage_exit(void) {
     fprintf(stderr, "Use -o output dir, -n N (x3), -s t0, -e T, -h dt, -c CFL, -v nu, -i IC, -t tag, -f forcing,\n"
-                    "    -p save every, -z checkpoint; -I ifrk4|rk4cn|rk5cn|dp5cn, -P fp64|fp32, -H, -a, -S seed, -k k0,\n"
+                    "    -p save every, -z checkpoint; -I rk4cn|ifrk4|rk5cn|dp5cn (default rk4cn), -P fp64|fp32,\n"
+                    "    -H (nu k^4, default) | -L (nu k^2), -a, -S seed, -k k0,\n"
                     "    -E energy, -F force_k, -R, -x\n"
                     "Example: ./solver -o ../Data/Tmp -n 64 -n 64 -n 64 -s 0.0 -e 1.0 -h 0.001 -v 0.0025 -i TAYLOR_GREEN\n");
     exit(1);
@@ -63,8 +64,12 @@ static void parse(int argc, char** argv, opts_t* o) {
     o->force_k = 2;
     o->k0 = 4.0;
     o->energy = 1.0;
+    /* the reference's default build (Makefile:44, data_types.h:57-71): RK4 +
+       Crank-Nicolson with hyperviscosity nu k^4 */
+    o->integ = NS3D_RK4CN;
+    o->hyper = 1;
     int c, dim = 0, outdir = 0;
-    while ((c = getopt(argc, argv, "o:h:n:d:s:e:t:v:i:c:p:f:z:I:P:HaS:k:E:F:Rx")) != -1) {
+    while ((c = getopt(argc, argv, "o:h:n:d:s:e:t:v:i:c:p:f:z:I:P:HLaS:k:E:F:Rx")) != -1) {
         switch (c) {
             case 'o':
                 if (outdir == 0) {
@@ -132,13 +137,14 @@ static void parse(int argc, char** argv, opts_t* o) {
                 }
                 break;
             case 'I':
-                o->integ = !strcmp(optarg, "rk4cn")   ? NS3D_RK4CN
+                o->integ = !strcmp(optarg, "ifrk4")   ? NS3D_IFRK4
                            : !strcmp(optarg, "rk5cn") ? NS3D_RK5CN
                            : !strcmp(optarg, "dp5cn") ? NS3D_DP5CN
-                                                      : NS3D_IFRK4;
+                                                      : NS3D_RK4CN;
                 break;
             case 'P': o->prec = !strcmp(optarg, "fp32") ? NS3D_FP32 : NS3D_FP64; break;
             case 'H': o->hyper = 1; break;
+            case 'L': o->hyper = 0; break;   /* nu k^2: the reference's "solver_test" build */
             case 'a': o->adaptive = 1; break;
             case 'S': o->seed = strtoull(optarg, NULL, 10); break;
             case 'k': o->k0 = atof(optarg); break;

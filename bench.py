@@ -28,12 +28,27 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 SAVE_EVERY = 100   # diagnostics cadence inside the timed steps (SAVE_EVERY of the reference's runs)
 sys.path.insert(0, ROOT)
 
-METRIC = "grid-pt*RK4-steps/s (512^3, FP32 bulk, forced turbulence)"
 UNIT = "grid-pt*steps/s"
-WORKLOAD = dict(workload="forced turbulence 512^3, FP32 bulk + FP64 integrating factors/reductions, IF-RK4, "
-                         "2/3 dealias, shell k<=2 energy forcing, CFL 0.5, SPECTRUM IC k0=4 seed 0",
-                N=512, nu=1e-3, cfl=0.5, k0=4.0, seed=0, forcing="shell k<=2", integrator="IF-RK4",
-                precision="fp32 bulk", l2="inputs larger than L2: each state field 369 MB > 129 MB L2")
+
+
+def nu_for(N: int) -> float:
+    """nu = 1e-3 at 512^3; the 1024^3 variant of the configuration runs nu = 4e-4."""
+    return 4e-4 if N >= 1024 else 1e-3
+
+
+def metric(N: int) -> str:
+    return f"grid-pt*RK4-steps/s ({N}^3, FP32 bulk, forced turbulence)"
+
+
+def workload(N: int) -> dict:
+    nu = nu_for(N)
+    nzp = (N // 3 + 1 + 7) // 8 * 8     # stored kz modes per (kx, ky) column
+    field_mb = N * N * nzp * 8 / 1e6     # one FP32 complex component
+    return dict(workload=f"forced turbulence {N}^3, FP32 bulk + FP64 integrating factors/reductions, IF-RK4, "
+                         f"2/3 dealias, shell k<=2 energy forcing, CFL 0.5, SPECTRUM IC k0=4 seed 0, nu={nu:g}",
+                N=N, nu=nu, cfl=0.5, k0=4.0, seed=0, forcing="shell k<=2", integrator="IF-RK4",
+                precision="fp32 bulk",
+                l2=f"inputs larger than L2: each state field {field_mb:.0f} MB > 129 MB L2")
 
 
 def parse():
@@ -48,7 +63,9 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
-    ap.add_argument("--workload", default="forced512", choices=["forced512", "ensemble", "les", "decay256", "closure-infer", "integrators"])
+    ap.add_argument("--workload", default="forced512",
+                    choices=["forced512", "ensemble", "les", "decay256", "closure-infer", "integrators", "fp32err512"])
+    ap.add_argument("--err-steps", type=int, default=1000)
     ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
     ap.add_argument("--les-steps", type=int, default=2000)
@@ -159,52 +176,59 @@ class Clocks:
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def cpu_baseline(N: int, seed: int = 0, nthreads: int = 0):
-    """Oracle (CPU FP64 restatement) timed on a bounded sample: one nonlinear
-    evaluation (NonlinearRHSBatch) at N^3, a quarter of an RK4 step."""
+def oracle_for(N: int, nthreads: int = 0):
+    """The oracle (CPU FP64 restatement) on the bench's configuration: IF-RK4,
+    CFL 0.5, shell k <= 2 forcing, SPECTRUM k0 = 4 seed 0."""
     from oracle import oracle as O
-    o = O.Oracle(N, nu=1e-3, dt=1e-3, nthreads=nthreads)
-    o.ic("SPECTRUM", seed=seed, k0=4.0, energy=1.0)
-    u = o.get_state()
+    O.build()
+    o = O.Oracle(N, nu=nu_for(N), dt=1e-3, cfl=0.5, forcing=O.FORCE_SHELL, force_k=2, nthreads=nthreads)
+    o.ic("SPECTRUM", seed=0, k0=4.0, energy=1.0)
+    return o, O.threads()
+
+
+def cpu_baseline(N: int):
+    """The oracle timed on a bounded sample of the workload: one whole RK4
+    step at N^3 (four nonlinear evaluations, the stage updates, the CFL step
+    and the forcing), after one untimed step."""
+    o, cores = oracle_for(N)
+    o.step(1)
     t0 = time.perf_counter()
-    o.rhs(u)
+    o.step(1)
     t = time.perf_counter() - t0
-    return {"value": N ** 3 / (4.0 * t), "unit": UNIT, "cores": O.threads(), "kind": "port",
-            "sample": f"one NonlinearRHSBatch at {N}^3 in FP64 ({t:.1f} s) = 1/4 of an RK4 step; "
-                      f"value = N^3 / (4 t); own mixed-radix FFT"}
+    return {"value": N ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"one whole IF-RK4 step at {N}^3 in FP64 ({t:.1f} s, after one untimed step), "
+                      f"oracle restatement with its own mixed-radix FFT, {cores} threads"}
 
 
 def run_reference(args, ws, rank):
-    """Reference arm: the CPU restatement of the reference's path (the reference
-    itself needs FFTW-MPI/MPI/HDF5 and cannot be built), all host threads."""
+    """Reference arm: the reference's CPU path on the host cores. The reference
+    program needs FFTW3-MPI, MPI and HDF5, which neither machine has, and its
+    compiled parts cannot travel to the Arm GPU host, so the arm times the
+    oracle restatement (pinned against the reference's own code), all host
+    threads. Each bench step is one RK4 stage of the workload (one nonlinear
+    evaluation and its stage update; every fourth stage also the final update
+    and the forcing): --steps K stages are K/4 RK4 steps, timed back to back
+    after --warmup W untimed stages."""
     if rank != 0:
         return
-    from oracle import oracle as O
-    O.build()
     N = args.N
-    o = O.Oracle(N, nu=1e-3, dt=1e-3, forcing=O.FORCE_SHELL, force_k=2)
-    o.ic("SPECTRUM", seed=0, k0=4.0, energy=1.0)
-    u = o.get_state()
-    # each step is a bounded sample: one nonlinear evaluation (1/4 of an RK4 step)
-    budget = 150.0
-    t_w = time.perf_counter()
-    o.rhs(u)
-    one = time.perf_counter() - t_w
-    steps = max(1, min(args.steps, int(budget / max(one, 1e-3))))
-    ts = []
-    for _ in range(steps):
-        t0 = time.perf_counter()
-        o.rhs(u)
-        ts.append(time.perf_counter() - t0)
-    t = sum(ts) / len(ts)
-    val = N ** 3 / (4.0 * t)
-    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": 1, "ms_per_step": 4000.0 * t, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(WORKLOAD, N=N),
-            "cpu_baseline": {"value": val, "unit": UNIT, "cores": O.threads(), "kind": "port",
-                             "sample": f"{steps} x one NonlinearRHSBatch at {N}^3 (1/4 RK4 step each); "
-                                       "value = N^3/(4 t)"},
+    o, cores = oracle_for(N)
+    for _ in range(args.warmup):
+        o.stage()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        o.stage()
+    t = time.perf_counter() - t0
+    val = N ** 3 * (args.steps / 4.0) / t
+    sample = (f"each bench step = one RK4 stage at {N}^3 in FP64 (1/4 of an RK4 step: a NonlinearRHSBatch and "
+              f"its stage update, every fourth with the final update and forcing); {args.steps} stages = "
+              f"{args.steps / 4:g} RK4 steps in {t:.1f} s; value = N^3 x (K/4) / t; oracle restatement, "
+              f"own mixed-radix FFT, {cores} threads")
+    line = {"impl": "reference", "metric": metric(N), "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload(N),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
             "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -219,9 +243,7 @@ def run_ours(args, ws, rank, local):
     torch.cuda.set_device(local)
     dist = Dist(ws, rank, local, True)
     N = args.N
-    # nu = 1e-3 at 512^3; the 1024^3 variant of the configuration runs nu = 4e-4
-    cfg = dict(nu=4e-4 if N >= 1024 else 1e-3, dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2,
-               device=local)
+    cfg = dict(nu=nu_for(N), dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
     tuned = None
     if not args.no_autotune:
         # the library's autotuner picks the tile / radix variant and z-pass form of this size (untimed)
@@ -236,19 +258,21 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     clk = Clocks(local)
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    # the metric's diagnostics: ComputeSystemMeasurables at every iteration that is a multiple
-    # of SAVE_EVERY = 100 (the reference's save cadence), inside the timed region
+    # the metric's diagnostics: ComputeSystemMeasurables once per SAVE_EVERY = 100 steps (the
+    # reference's save cadence), inside the timed region, and at least once in any window
+    # (K < 100 steps are charged a whole call)
+    saves = max(1, round(args.steps / SAVE_EVERY))
+    every = args.steps // saves
     ev0.record(stream)
-    done, it, saves, lib_ms = 0, args.warmup, 0, 0.0
+    done, lib_ms, made = 0, 0.0, 0
     while done < args.steps:
-        n = min(args.steps - done, SAVE_EVERY - it % SAVE_EVERY)
+        n = min(args.steps - done, every)
         s.RK4Step(n)
         lib_ms += s.last_step_ms()
         done += n
-        it += n
-        if it % SAVE_EVERY == 0:
+        if made < saves and (done % every == 0 or done == args.steps):
             s.ComputeSystemMeasurables()
-            saves += 1
+            made += 1
     ev1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()
@@ -315,7 +339,8 @@ def run_ours(args, ws, rank, local):
 
     fp64 = None
     if not args.no_fp64:
-        s64 = pkg.Solver(N, nu=1e-3, dt=1e-3, cfl=0.5, precision="fp64", forcing="SHELL", force_k=2, device=local)
+        s64 = pkg.Solver(N, nu=nu_for(N), dt=1e-3, cfl=0.5, precision="fp64", forcing="SHELL", force_k=2,
+                         device=local)
         s64.InitialConditions("SPECTRUM", seed=0, k0=4.0, energy=1.0)
         s64.RK4Step(1)
         torch.cuda.synchronize()
@@ -332,12 +357,12 @@ def run_ours(args, ws, rank, local):
     dist.close()
     if rank != 0:
         return
-    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+    line = {"metric": metric(N), "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": dict(WORKLOAD, N=N, parallelism=f"replicas x{ws}", autotune=tuned,
-                           diagnostics=f"ComputeSystemMeasurables every {SAVE_EVERY} iterations inside the "
-                                       f"timed steps ({saves} call(s) in this run)"),
+            "config": dict(workload(N), parallelism=f"replicas x{ws}", autotune=tuned,
+                           diagnostics=f"ComputeSystemMeasurables once per {SAVE_EVERY} steps inside the timed "
+                                       f"steps, at least once per window ({saves} call(s) in {args.steps} steps)"),
             "clocks": clocks, "e2e": e2e, "gpu_launches": s_kernels(pkg, N) * args.steps + 2 * saves,
             "roofline": roofline, "cpu_baseline": cpu, "fp64": fp64,
             "library_ms_per_step": lib_ms / args.steps,
@@ -518,6 +543,55 @@ def run_decay(args, local):
     print(json.dumps(line), flush=True)
 
 
+def run_fp32err(args, local):
+    """Config C3's accuracy bar: forced turbulence at N^3 (default 512^3; SPECTRUM IC k0 = 4 seed 0,
+    nu = 1e-3, CFL 0.5, shell k <= 2 forcing, IF-RK4) for --err-steps steps (default 1000) in FP64 and
+    in FP32 bulk from the same initial field; the FP32 relative errors of the energy, the dissipation
+    and every E(k) shell against FP64, every 100 steps and at the end, and both step rates."""
+    import importlib
+    import numpy as np
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    pkg.tuning_load(os.path.join(ROOT, "3d_navier_stokes_gb300", "tuning", "gb300.txt"))
+    N, steps = args.N, args.err_steps
+    every = 100 if steps >= 100 else steps
+    res = {}
+    for prec in ("fp64", "fp32"):
+        s = pkg.Solver(N, nu=nu_for(N), dt=1e-3, cfl=0.5, precision=prec, forcing="SHELL", force_k=2, device=local)
+        s.InitialConditions("SPECTRUM", seed=0, k0=4.0)
+        series, ms = [], 0.0
+        done = 0
+        while done < steps:
+            n = min(every, steps - done)
+            s.RK4Step(n)
+            ms += s.last_step_ms()
+            done += n
+            tot, Ek, _ = s.ComputeSystemMeasurables()
+            series.append((done, s.get_time()[0], tot["energy"], tot["dissipation"], Ek))
+        res[prec] = (series, ms / steps)
+        s.close()
+    kk = np.arange(1, N // 3 + 1)
+    rows = []
+    for a, b in zip(res["fp64"][0], res["fp32"][0]):
+        rows.append({"steps": a[0], "t_fp64": a[1], "t_fp32": b[1],
+                     "energy_rel_err": abs(b[2] - a[2]) / a[2],
+                     "dissipation_rel_err": abs(b[3] - a[3]) / a[3],
+                     "Ek_max_rel_err": float(np.max(np.abs(b[4][kk] - a[4][kk]) / a[4][kk]))})
+    last = rows[-1]
+    line = {"metric": f"FP32 vs FP64 relative energy error after {steps} steps, {N}^3 forced turbulence",
+            "value": last["energy_rel_err"], "unit": "relative error", "higher_is_better": False,
+            "target": 1e-5, "steps": steps, "n_gpus": 1, "data": "synthetic", "dtype": "f32 vs f64",
+            "dissipation_rel_err": last["dissipation_rel_err"], "Ek_max_rel_err_all_shells": last["Ek_max_rel_err"],
+            "max_over_checkpoints": {k: max(r[k] for r in rows) for k in
+                                     ("energy_rel_err", "dissipation_rel_err", "Ek_max_rel_err")},
+            "series": rows, "ms_per_step": {"fp64": res["fp64"][1], "fp32": res["fp32"][1]},
+            "fp32_over_fp64_speed": res["fp64"][1] / res["fp32"][1],
+            "config": dict(workload(N), shells=f"k = 1..{N // 3}")}
+    print(json.dumps(line), flush=True)
+
+
 def run_rk5(args, local):
     """The integrators of the step at N^3 (default 512^3) FP32 with shell forcing: IF-RK4,
     RK4CN (CFL 0.5), RK5CN (CFL 0.5, 6 RHS per step) and DP5CN (Dormand-Prince step
@@ -578,6 +652,9 @@ def main():
         return
     if args.workload == "integrators":
         run_rk5(args, local)
+        return
+    if args.workload == "fp32err512":
+        run_fp32err(args, local)
         return
     run_ours(args, ws, rank, local)
 

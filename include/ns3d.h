@@ -129,14 +129,18 @@ ns3d_status ns3d_real_space_host(ns3d_ctx* ctx, double* u, double* w);
 
 /* ComputeSystemMeasurables for callers that cannot allocate device memory
  * (no counterpart in the reference). Input: a device array in the reference
- * Fourier layout, complex double [N][N][N/2+1][3]; every mode counts, as in
- * the reference. Outputs (device): d_totals[5] in the order of ns3d_measures,
- * and n_spect doubles each in d_Ek / d_Ok (either may be NULL). Runs
- * asynchronously on `stream` (NULL = default stream). Its partial sums live in
- * a 2 MiB static device array shared by every call, so N <= 512 (larger N:
- * NS3D_ERR_INVALID) and calls that overlap on the GPU race. The first call on
- * a device resolves that array's address; make it before any stream capture.
- * Allocates nothing. */
+ * Fourier layout, complex double [N][N][N/2+1][3], 16-byte aligned; every mode
+ * counts, as in the reference, except that shells with round(|k|) >= n_spect
+ * (corner modes that the reference writes past its spectrum arrays for) are
+ * left out of d_Ek / d_Ok while staying in the totals. Outputs (device):
+ * d_totals[5] in the order of ns3d_measures, and n_spect doubles each in
+ * d_Ek / d_Ok (either may be NULL). Runs asynchronously on `stream` (NULL =
+ * default stream). Its partial sums live in a 2 MiB static device array
+ * shared by every call, so N <= 512 (larger N: NS3D_ERR_INVALID) and calls
+ * that overlap on the GPU race. Outside stream capture each call resolves that
+ * array's address in the current context; a call under capture reuses the one
+ * resolved earlier in the same context, so make one call per context (again
+ * after a cudaDeviceReset) before capturing. Allocates nothing. */
 ns3d_status ns3d_measurables_noalloc(int N, double nu, int visc_pow, const double* d_u_hat,
                                      double* d_totals, double* d_Ek, double* d_Ok, void* stream);
 
@@ -153,6 +157,16 @@ ns3d_status ns3d_set_forcing_target(ns3d_ctx* ctx, double e);
  * returns after n accepted steps; n steps rejected DP_MAX_TRY = 50 times in a
  * row end it with NS3D_ERR_NUMERIC. */
 ns3d_status ns3d_set_dp_tolerances(ns3d_ctx* ctx, double atol, double rtol);
+
+/* Failure detection (no counterpart in the reference, whose limits
+ * MIN_STEP_SIZE, MAX_ITERS and MAX_VORT_LIM at data_types.h:130-136 are
+ * defined but never checked). Every wait of the z pass on an asynchronous
+ * copy is bounded: after `cycles` SM clock cycles (<= 0: the default, 4e9,
+ * about 2 s) the pass records a timeout, lets its copies in flight land and
+ * returns, and ns3d_step reports NS3D_ERR_TIMEOUT. A short budget makes that
+ * path fire on purpose (tests); ns3d_set_time clears the recorded status.
+ * A NaN or Inf in the field is reported by ns3d_step as NS3D_ERR_NUMERIC. */
+ns3d_status ns3d_set_wait_budget(ns3d_ctx* ctx, long long cycles);
 ns3d_status ns3d_dp_stats(ns3d_ctx* ctx, double* last_err, long* rejects);
 
 /* Longitudinal velocity-increment statistics of the current state, the

@@ -41,9 +41,14 @@ typedef struct system_vars_struct {
     double CFL_CONST;
     double NU;
     int SAVE_EVERY;
-    /* switches that the reference sets at compile time (Makefile:43-53) */
-    int hyper_visc;        /* 1: nu k^4 (HYPER_VISC, VIS_POW 2.0)             */
-    int integrator;        /* 0: IF-RK4, 1: RK4 + Crank-Nicolson (RK4Step),
+    /* switches that the reference sets at compile time (Makefile:43-53); a
+       zero-filled struct gives the reference's default build ("solver":
+       -D__NAVIER -D__HYPER with data_types.h's __RK4) */
+    int visc_pow;          /* 0: the default build's hyperviscosity nu k^4
+                              (HYPER_VISC, VIS_POW 2.0, data_types.h:68-71);
+                              1: nu k^2 (the "solver_test" build); 2: nu k^4 */
+    int integrator;        /* 0: RK4 + Crank-Nicolson (RK4Step, solver.c:505-608),
+                              1: integrating-factor RK4 (no reference counterpart),
                               2: RK5 (__RK5), 3: Dormand-Prince (__DPRK5)      */
     int precision;         /* 0: FP64, 1: FP32 bulk                          */
     int adaptive_step;     /* 1: CFL step (__ADAPTIVE_STEP)                   */
@@ -79,7 +84,11 @@ extern runtime_data_struct* run_data;
 void InitializeSpaceVariables(double** x, int** k, const long int* N);
 /* solver.c:1537-1648 (TAYLOR_GREEN, SHAPIRO, TESTING, RANDOM/other, SPECTRUM) */
 void InitialConditions(ns3d_fftw_complex* u_hat, double* u, const long int* N);
-/* solver.c:505-608: one step of run_data->u_hat in place */
+/* solver.c:505-608: one step of run_data->u_hat in place. The device state
+   holds only the modes inside the 2/3 sphere: modes outside it in the host
+   array are dropped on input and come back as zeros (the reference's RK4Step
+   on an array that was never dealiased keeps them and decays them by the
+   Crank-Nicolson factor; after any NonlinearRHSBatch the two agree). */
 void RK4Step(const double dt, const long int* N, const ptrdiff_t local_Nx, RK_data_struct* RK_data);
 /* solver.c:217-421 (integrator 2 or 3; for 3 one accepted adaptive step) */
 void RK5DPStep(const double dt, const long int* N, const int iters, const ptrdiff_t local_Nx, RK_data_struct* RK_data);

@@ -199,6 +199,7 @@ struct orc_ctx {
     long dp_rejects;
     double t, dt;
     long iters;
+    int stage;               /* next stage of orc_stage (0..3) */
     double force_target;
     double last_umax;        /* max(|u|+|v|+|w|) seen by the last stage-1 RHS */
 };
@@ -289,7 +290,12 @@ void orc_set_state(orc_ctx* c, const double* u_hat) {
 void orc_get_state(const orc_ctx* c, double* u_hat) {
     memcpy(u_hat, c->u_hat, sizeof(cplx) * 3 * (size_t)c->nF);
 }
-void orc_set_time(orc_ctx* c, double t, double dt, long iters) { c->t = t; c->dt = dt; c->iters = iters; }
+void orc_set_time(orc_ctx* c, double t, double dt, long iters) {
+    c->t = t;
+    c->dt = dt;
+    c->iters = iters;
+    c->stage = 0;
+}
 void orc_get_time(const orc_ctx* c, double* t, double* dt, long* iters) {
     if (t) *t = c->t;
     if (dt) *dt = c->dt;
@@ -539,71 +545,99 @@ static void apply_forcing(orc_ctx* c) {
         for (int j = 0; j < N; ++j)                                 \
             for (int k = 0; k < NF; ++k)
 
-static void one_step(orc_ctx* c) {
+/* One stage s = 0..3 of a step: the stage's nonlinear evaluation and the
+   stage algebra that follows it; stage 3 ends with the final update, the
+   forcing and the time bookkeeping. */
+static void stage_step(orc_ctx* c, int st) {
     const int N = c->N, NF = c->NF;
     cplx* u = c->u_hat;
     const int cfl = c->p.cfl > 0.0;
-    rhs_impl(c, u, c->rk1, cfl);
-    if (cfl) {
-        if (c->last_umax > 0.0) c->dt = c->p.cfl * (2.0 * M_PI / (double)N) / c->last_umax;
+    if (st == 0) {
+        rhs_impl(c, u, c->rk1, cfl);
+        if (cfl) {
+            if (c->last_umax > 0.0) c->dt = c->p.cfl * (2.0 * M_PI / (double)N) / c->last_umax;
+        }
     }
     const double h = c->dt;
     if (c->p.integrator == ORC_RK4CN) {
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk1[x + d];
-        }
-        rhs_impl(c, c->rk_tmp, c->rk2, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk2[x + d];
-        }
-        rhs_impl(c, c->rk_tmp, c->rk3, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 1.0 * c->rk3[x + d];
-        }
-        rhs_impl(c, c->rk_tmp, c->rk4, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            double D = h * visc(c, i, j, k);
-            for (int d = 0; d < 3; ++d)
-                u[x + d] = u[x + d] * ((2.0 - D) / (2.0 + D)) +
-                           (2.0 * h / (2.0 + D)) * (1.0 / 6.0 * c->rk1[x + d] + 1.0 / 3.0 * c->rk2[x + d] +
-                                                    1.0 / 3.0 * c->rk3[x + d] + 1.0 / 6.0 * c->rk4[x + d]);
+        if (st == 0) {
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk1[x + d];
+            }
+        } else if (st == 1) {
+            rhs_impl(c, c->rk_tmp, c->rk2, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 0.5 * c->rk2[x + d];
+            }
+        } else if (st == 2) {
+            rhs_impl(c, c->rk_tmp, c->rk3, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = u[x + d] + h * 1.0 * c->rk3[x + d];
+            }
+        } else {
+            rhs_impl(c, c->rk_tmp, c->rk4, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double D = h * visc(c, i, j, k);
+                for (int d = 0; d < 3; ++d)
+                    u[x + d] = u[x + d] * ((2.0 - D) / (2.0 + D)) +
+                               (2.0 * h / (2.0 + D)) * (1.0 / 6.0 * c->rk1[x + d] + 1.0 / 3.0 * c->rk2[x + d] +
+                                                        1.0 / 3.0 * c->rk3[x + d] + 1.0 / 6.0 * c->rk4[x + d]);
+            }
         }
     } else {
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            double E = exp(-0.5 * h * visc(c, i, j, k));
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * (u[x + d] + 0.5 * h * c->rk1[x + d]);
-        }
-        rhs_impl(c, c->rk_tmp, c->rk2, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            double E = exp(-0.5 * h * visc(c, i, j, k));
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * u[x + d] + 0.5 * h * c->rk2[x + d];
-        }
-        rhs_impl(c, c->rk_tmp, c->rk3, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            double E = exp(-0.5 * h * visc(c, i, j, k));
-            for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * E * u[x + d] + h * E * c->rk3[x + d];
-        }
-        rhs_impl(c, c->rk_tmp, c->rk4, 0);
-        FOR_MODES {
-            long x = 3 * ((long)(i * N + j) * NF + k);
-            double E = exp(-0.5 * h * visc(c, i, j, k));
-            double E2 = E * E;
-            for (int d = 0; d < 3; ++d)
-                u[x + d] = E2 * u[x + d] +
-                           h / 6.0 * (E2 * c->rk1[x + d] + 2.0 * E * (c->rk2[x + d] + c->rk3[x + d]) + c->rk4[x + d]);
+        if (st == 0) {
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double E = exp(-0.5 * h * visc(c, i, j, k));
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * (u[x + d] + 0.5 * h * c->rk1[x + d]);
+            }
+        } else if (st == 1) {
+            rhs_impl(c, c->rk_tmp, c->rk2, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double E = exp(-0.5 * h * visc(c, i, j, k));
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * u[x + d] + 0.5 * h * c->rk2[x + d];
+            }
+        } else if (st == 2) {
+            rhs_impl(c, c->rk_tmp, c->rk3, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double E = exp(-0.5 * h * visc(c, i, j, k));
+                for (int d = 0; d < 3; ++d) c->rk_tmp[x + d] = E * E * u[x + d] + h * E * c->rk3[x + d];
+            }
+        } else {
+            rhs_impl(c, c->rk_tmp, c->rk4, 0);
+            FOR_MODES {
+                long x = 3 * ((long)(i * N + j) * NF + k);
+                double E = exp(-0.5 * h * visc(c, i, j, k));
+                double E2 = E * E;
+                for (int d = 0; d < 3; ++d)
+                    u[x + d] = E2 * u[x + d] +
+                               h / 6.0 * (E2 * c->rk1[x + d] + 2.0 * E * (c->rk2[x + d] + c->rk3[x + d]) + c->rk4[x + d]);
+            }
         }
     }
-    if (c->p.forcing == ORC_FORCE_SHELL) apply_forcing(c);
-    c->iters += 1;
-    if (cfl) c->t += h;
-    else c->t = c->p.t0 + (double)c->iters * h;
+    if (st == 3) {
+        if (c->p.forcing == ORC_FORCE_SHELL) apply_forcing(c);
+        c->iters += 1;
+        if (cfl) c->t += h;
+        else c->t = c->p.t0 + (double)c->iters * h;
+    }
+}
+
+static void one_step(orc_ctx* c) {
+    for (int st = 0; st < 4; ++st) stage_step(c, st);
+}
+
+int orc_stage(orc_ctx* c) {
+    if (c->p.integrator != ORC_IFRK4 && c->p.integrator != ORC_RK4CN) return -1;
+    stage_step(c, c->stage);
+    c->stage = (c->stage + 1) & 3;
+    return c->stage;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -934,6 +968,7 @@ int orc_ic(orc_ctx* c, const char* name, uint64_t seed, double k0, double energy
     c->t = c->p.t0;
     c->dt = c->p.dt;
     c->iters = 0;
+    c->stage = 0;
     if (c->p.forcing == ORC_FORCE_SHELL) c->force_target = energy_shells(c, uh, c->p.force_k);
     return 0;
 }

@@ -67,6 +67,10 @@ void orc_dealias(orc_ctx* c, double* arr, int array_dim);
 void orc_rhs(orc_ctx* c, const double* u_hat, double* rhs);
 /* returns 0, or 1 when a DP5CN step was rejected DP_MAX_TRY = 50 times in a row */
 int  orc_step(orc_ctx* c, int nsteps);
+/* One RK4 stage (IF-RK4 or RK4CN): the stage's nonlinear evaluation and its
+   stage update; every fourth call also the final update, forcing and time.
+   Returns the next stage (0 after a completed step), -1 for other integrators. */
+int  orc_stage(orc_ctx* c);
 /* DP5CN: error norm of the last attempt, rejected attempts so far */
 void orc_dp_stats(const orc_ctx* c, double* last_err, long* rejects);
 void orc_measurables(orc_ctx* c, double* totals5, double* Ek, double* Ok);

@@ -76,6 +76,8 @@ def lib():
         L.orc_fft1d.argtypes = [ctypes.c_int, D, D, ctypes.c_int]
         L.orc_dealias.argtypes = [P, D, ctypes.c_int]
         L.orc_rhs.argtypes = [P, D, D]
+        L.orc_stage.argtypes = [P]
+        L.orc_stage.restype = ctypes.c_int
         L.orc_step.argtypes = [P, ctypes.c_int]
         L.orc_step.restype = ctypes.c_int
         L.orc_dp_stats.argtypes = [P, ctypes.c_void_p, ctypes.c_void_p]
@@ -191,6 +193,13 @@ class Oracle:
     def step(self, n=1):
         if lib().orc_step(self._c, n) != 0:
             raise RuntimeError("DP5CN step rejected 50 times in a row")
+
+    def stage(self) -> int:
+        """One RK4 stage (IF-RK4 / RK4CN); returns the next stage, 0 after a completed step."""
+        r = lib().orc_stage(self._c)
+        if r < 0:
+            raise RuntimeError("orc_stage: IF-RK4 and RK4CN only")
+        return r
 
     def increment_stats(self, increments=None, n_bins=1000):
         """Longitudinal velocity-increment statistics, bin edges and counts

@@ -2,9 +2,11 @@
  * A reference-shaped driver: the loop of SpectralSolve (solver.c:50-208)
  * written against include/ns3d_compat.h, i.e. the reference's function names
  * and global structs. Used by tests/test_driver_compat.py.
- *   compat_driver N nu dt nsteps integrator(0..3) out.bin
- * Integrators 0 and 1 step with RK4Step, 2 and 3 with RK5DPStep (for 3 the
- * step size follows the Dormand-Prince control through sys_vars->dt).
+ *   compat_driver N nu dt nsteps integrator(0..3) visc_pow(0..2) out.bin
+ * The switches are written into the zero-filled sys_vars as given (0 0 is the
+ * reference's default build: RK4 + Crank-Nicolson, nu k^4). Integrators 0
+ * and 1 step with RK4Step, 2 and 3 with RK5DPStep (for 3 the step size
+ * follows the Dormand-Prince control through sys_vars->dt).
  * Writes u_hat after nsteps (complex double [N][N][N/2+1][3]) followed by the
  * energy/enstrophy series recorded after every step, then sys_vars->t and
  * sys_vars->dt (set by RK5DPStep for integrator 3).
@@ -16,7 +18,7 @@
 #include "ns3d_compat.h"
 
 int main(int argc, char** argv) {
-    if (argc != 7) return 2;
+    if (argc != 8) return 2;
     system_vars_struct sv;
     runtime_data_struct rd;
     RK_data_struct rk;
@@ -31,6 +33,7 @@ int main(int argc, char** argv) {
     sv.NU = atof(argv[2]);
     sv.dt = atof(argv[3]);
     sv.integrator = atoi(argv[5]);
+    sv.visc_pow = atoi(argv[6]);
     strcpy(sv.u0, "TAYLOR_GREEN");
     strcpy(sv.forcing, "NONE");
     const long NF = N / 2 + 1;
@@ -54,7 +57,7 @@ int main(int argc, char** argv) {
             RK4Step(sv.dt, sv.N, sv.local_Nx, &rk);
         ComputeSystemMeasurables(it);
     }
-    FILE* f = fopen(argv[6], "wb");
+    FILE* f = fopen(argv[7], "wb");
     fwrite(rd.u_hat, sizeof(ns3d_fftw_complex), N * N * NF * 3, f);
     fwrite(rd.tot_energy, sizeof(double), steps + 1, f);
     fwrite(rd.tot_enstr, sizeof(double), steps + 1, f);

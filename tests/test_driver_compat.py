@@ -35,8 +35,10 @@ def test_driver_rejects_bad_arguments(ns3d):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("integrator", [0, 1, 2, 3])
-def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator):
+@pytest.mark.parametrize("integrator,visc_pow", [(0, 0), (0, 1), (1, 1), (2, 1), (3, 1), (1, 2)])
+def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator, visc_pow):
+    """(0, 0) is a zero-filled sys_vars: the reference's default build, RK4 +
+    Crank-Nicolson with nu k^4."""
     exe = tmp_path / "compat_driver"
     libdir = os.path.dirname(ns3d.LIB_PATH)
     subprocess.run(["gcc", "-std=gnu11", "-O2", "-I", os.path.join(ROOT, "include"),
@@ -44,12 +46,14 @@ def test_compat_shim_reference_shaped_driver(ns3d, oracle, tmp_path, integrator)
                     f"-Wl,-rpath,{libdir}"], check=True)
     N, nu, dt, n = 24, 0.01, 2e-3, 5
     out = tmp_path / "out.bin"
-    subprocess.run([str(exe), str(N), str(nu), str(dt), str(n), str(integrator), str(out)], check=True)
+    subprocess.run([str(exe), str(N), str(nu), str(dt), str(n), str(integrator), str(visc_pow), str(out)],
+                   check=True)
     raw = np.fromfile(out, dtype=np.float64)
     nf = N * N * (N // 2 + 1) * 3
     u = raw[:2 * nf].view(np.complex128).reshape(N, N, N // 2 + 1, 3)
     E = raw[2 * nf:2 * nf + n + 1]
-    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=[oracle.IFRK4, oracle.RK4CN, oracle.RK5CN, oracle.DP5CN][integrator])
+    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=[oracle.RK4CN, oracle.IFRK4, oracle.RK5CN, oracle.DP5CN][integrator],
+                      visc_pow=1 if visc_pow == 1 else 2)
     o.ic("TAYLOR_GREEN")
     ref_E = [o.measurables()[0][0]]
     for _ in range(n):
@@ -71,7 +75,7 @@ def test_driver_outputs_match_oracle(ns3d, oracle, tmp_path):
     exe = solver_bin(ns3d)
     N, nu, dt = 32, 0.01, 2e-3
     args = [exe, "-o", str(tmp_path), "-n", str(N), "-n", str(N), "-n", str(N), "-s", "0.0", "-e", "0.02",
-            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "5", "-t", "T1"]
+            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "5", "-t", "T1", "-I", "ifrk4", "-L"]
     r = subprocess.run(args, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     sub = [d for d in os.listdir(tmp_path) if d.startswith("SIM_DATA_NAVIER_IFRK4_FULL_N[32,32]")]
@@ -106,7 +110,7 @@ def test_driver_rk5_integrators_match_oracle(ns3d, oracle, tmp_path, integ):
     exe = solver_bin(ns3d)
     N, nu, dt, T = 32, 0.01, 2e-3, 0.02
     args = [exe, "-o", str(tmp_path), "-n", str(N), "-n", str(N), "-n", str(N), "-s", "0.0", "-e", str(T),
-            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "1", "-I", integ, "-t", "R5"]
+            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "1", "-I", integ, "-t", "R5", "-L"]
     r = subprocess.run(args, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     tag = {"rk5cn": "RK5", "dp5cn": "DP5"}[integ]
@@ -132,6 +136,29 @@ def test_driver_rk5_integrators_match_oracle(ns3d, oracle, tmp_path, integ):
         assert len(Ts) == 11 and np.allclose(steps, dt, rtol=1e-9)
     else:
         assert np.ptp(steps) > 1e-3 * dt   # the control changed the step size
+
+
+@pytest.mark.gpu
+def test_driver_defaults_are_the_reference_build(ns3d, oracle, tmp_path):
+    """With no integrator or viscosity flag the binary runs what the
+    reference's default build runs: RK4 + Crank-Nicolson (RK4Step,
+    solver.c:505-608) with hyperviscosity nu k^4 (Makefile:44)."""
+    exe = solver_bin(ns3d)
+    N, nu, dt = 16, 1e-3, 2e-3
+    args = [exe, "-o", str(tmp_path), "-n", str(N), "-n", str(N), "-n", str(N), "-s", "0.0", "-e", "0.01",
+            "-h", str(dt), "-v", str(nu), "-i", "TAYLOR_GREEN", "-p", "5", "-t", "D"]
+    r = subprocess.run(args, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    sub = [d for d in os.listdir(tmp_path) if d.startswith("SIM_DATA_NAVIER_RK4_FULL_N[16,16]")]
+    assert len(sub) == 1, os.listdir(tmp_path)
+    main = read_container(os.path.join(tmp_path, sub[0], "Main_HDF_Data.ns3d"))
+    o = oracle.Oracle(N, nu=nu, dt=dt, integrator=oracle.RK4CN, visc_pow=2)
+    o.ic("TAYLOR_GREEN")
+    o.step(5)
+    u5, _ = main["/Iter_00005/u_hat"]
+    ref = o.get_state()
+    assert np.linalg.norm(u5 - ref) / np.linalg.norm(ref) < 1e-12
+    assert main["/EnergyDissipation"][0][-1] == pytest.approx(o.measurables()[0][4], rel=1e-12)
 
 
 @pytest.mark.gpu

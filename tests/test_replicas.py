@@ -56,4 +56,6 @@ def test_reference_arm_runs_on_rank_zero_only():
     assert len(lines) == 1
     line = lines[0]
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
+    # the line reports the steps and warm-up it ran, and ms_per_step x steps is its timed time
+    assert line["steps"] == 1 and line["warmup"] == 1
     assert line["cpu_baseline"]["kind"] == "port" and line["e2e"]["h2d_bytes_per_step"] == 0
