@@ -64,7 +64,8 @@ class Base {
     virtual ns3d_status les_counters(long* on, long* off) = 0;
     virtual const float* real_velocity_f32(ns3d_status* st) = 0;
     virtual ns3d_status set_state_real_host(const double* u) = 0;
-    // z-pass form: 0 the persistent line kernel where compiled, 1 the CTA-synchronous pass
+    // z-pass form: 0 the persistent line kernel where compiled, 1 the CTA-synchronous pass,
+    // 2 the tensor-core GEMMs where compiled
     virtual void set_zform(int z) = 0;
     virtual int zform() const = 0;
     virtual int variant() const = 0;
@@ -101,6 +102,10 @@ Base* make_f64_large(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f32_v6(int N, const ns3d_params* ps, int M, cudaStream_t s);
 Base* make_f64_v0(int N, const ns3d_params* ps, int M, cudaStream_t s);
 bool supported_n(int N);
+// z-pass form 2 (tensor-core GEMMs, zgemm.cuh) exists for FP32 and N in {16, 32, 48, 64, 96, 128}
+inline bool zgemm_size(int N, int precision) {
+    return precision == NS3D_FP32 && N >= 16 && N <= 128 && N % 16 == 0;
+}
 constexpr int kTileVariants = 7;   // TileVar<0..6>, PlansV (ns3d_kernels.cuh)
 
 inline unsigned long long host_splitmix64(unsigned long long x) {

@@ -74,7 +74,8 @@ class Impl final : public Base {
         if (graph_exec_) cudaGraphExecDestroy(graph_exec_);
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
                         (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
-                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_out_.ranges, (void*)plan_in_.ranges})
+                        (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_out_.ranges, (void*)plan_in_.ranges,
+                        (void*)zg_b_, (void*)zg_P_})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -85,9 +86,10 @@ class Impl final : public Base {
     bool rk5() const { return p_.integrator == INT_RK5CN || p_.integrator == INT_DP5CN; }
     bool dp5() const { return p_.integrator == INT_DP5CN; }
     int kernels_per_step() const override {
-        if (dp5()) return 1 + 7 * 5 + 3;
-        if (rk5()) return 6 * 5 + (p_.cfl > 0 ? 1 : 0) + 1;
-        return 4 * 5 + (p_.cfl > 0 ? 1 : 0) + 1;
+        const int z2 = zform_ == 2 ? 1 : 0;   // the tensor-core z pass is two kernels
+        if (dp5()) return 1 + 7 * (5 + z2) + 3;
+        if (rk5()) return 6 * (5 + z2) + (p_.cfl > 0 ? 1 : 0) + 1;
+        return 4 * (5 + z2) + (p_.cfl > 0 ? 1 : 0) + 1;
     }
 
     ns3d_status init() override {
@@ -144,6 +146,20 @@ class Impl final : public Base {
         }
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
         NS3D_CK(cudaFuncSetAttribute(k_zpass<T, N, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_z()));
+        if constexpr (zgemm_ok<T, N>()) {
+            // z-pass form 2: DFT matrices (built once, on the host), the product workspace
+            using Z = ZGeo<N>;
+            NS3D_CK(cudaFuncSetAttribute(k_zgemm_inv<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM_INV));
+            NS3D_CK(cudaFuncSetAttribute(k_zgemm_fwd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, Z::SMEM_FWD));
+            std::vector<uint16_t> mats(2 * (size_t)N * Z::KI * 2);
+            zgemm_matrices(N, Z::KI, mats.data());
+            NS3D_CK(cudaMalloc(&zg_b_, sizeof(uint16_t) * mats.size()));
+            NS3D_CK(cudaMemcpyAsync(zg_b_, mats.data(), sizeof(uint16_t) * mats.size(), cudaMemcpyHostToDevice, s_));
+            NS3D_CK(cudaMalloc(&zg_P_, sizeof(float) * 3 * (size_t)N * N * N * M_));
+            int dev = 0;
+            NS3D_CK(cudaGetDevice(&dev));
+            NS3D_CK(cudaDeviceGetAttribute(&zg_ctas_, cudaDevAttrMultiProcessorCount, dev));
+        }
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
         NS3D_CK(cudaFuncSetAttribute(k_xfwd<T, N, INT_TAB, X_STAGE1, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -182,6 +198,19 @@ class Impl final : public Base {
     }
     static constexpr size_t smem_zl() { return zline_smem<T, N>(); }
     void p3(int want_umax, int m0, int cnt) {
+        if constexpr (zgemm_ok<T, N>()) {
+            if (zform_ == 2) {
+                using Z = ZGeo<N>;
+                const long long tiles = (long long)N * N * cnt / 128;
+                const unsigned grid = (unsigned)(tiles < zg_ctas_ ? tiles : zg_ctas_);
+                float* P = zg_P_ + (size_t)m0 * 3 * N * N * N;
+                k_zgemm_inv<N><<<grid, kZgThreads, Z::SMEM_INV, s_>>>(reinterpret_cast<const float*>(Wm(m0)), zg_b_,
+                                                                      P, sdm(m0), want_umax, cnt);
+                k_zgemm_fwd<N><<<grid, kZgThreads, Z::SMEM_FWD, s_>>>(P, zg_b_ + 2 * Z::BI / 16,
+                                                                      reinterpret_cast<float*>(Wm(m0)), sdm(m0), cnt);
+                return;
+            }
+        }
         if constexpr (zline_ok<T, N>()) {
             if (zform_ == 0) {
                 // persistent: as many CTAs as fit on the device, never more than there are line groups
@@ -198,7 +227,7 @@ class Impl final : public Base {
             Wm(m0), tw_, nullptr, sdm(m0), want_umax);
     }
     void set_zform(int z) override {
-        const int zn = (zline_ok<T, N>() && z == 0) ? 0 : 1;
+        const int zn = (zline_ok<T, N>() && z == 0) ? 0 : (zgemm_ok<T, N>() && z == 2) ? 2 : 1;
         if (zn != zform_ && graph_exec_) {
             cudaGraphExecDestroy(graph_exec_);
             graph_exec_ = nullptr;
@@ -412,8 +441,9 @@ class Impl final : public Base {
             set_err("per-kernel profile covers the RK4-family step");
             return NS3D_ERR_UNSUPPORTED;
         }
-        const char* kNames[6] = {"k_xinv", "k_ypass_inv", zform_ == 0 ? "k_zline" : "k_zpass", "k_ypass_fwd", "k_xfwd",
-                                 "k_misc"};
+        const char* kNames[6] = {"k_xinv", "k_ypass_inv",
+                                 zform_ == 0 ? "k_zline" : zform_ == 2 ? "k_zgemm" : "k_zpass", "k_ypass_fwd",
+                                 "k_xfwd", "k_misc"};
         std::vector<cudaEvent_t> ev(2 * 6 * 4 + 2);
         for (auto& e : ev) NS3D_CK(cudaEventCreate(&e));
         double acc[6] = {0, 0, 0, 0, 0, 0};
@@ -1007,6 +1037,9 @@ class Impl final : public Base {
     cx<T>* TAU_ = nullptr;         // tau_ij spectra (6 fields)
     cx<T>* F_ = nullptr;           // -div(tau) (3 fields)
     T* tau_real_ = nullptr;        // tau_ij in real space [6][N^3]
+    uint4* zg_b_ = nullptr;        // z-pass form 2: DFT matrices (Binv hi, lo, Bfwd hi, lo)
+    float* zg_P_ = nullptr;        // z-pass form 2: the three real-space products [member][3][N^3]
+    int zg_ctas_ = 0;
     double* sgs_part_ = nullptr;
     cx<T>* K_ = nullptr;           // RK5 family: stored stages [member][6][3]
     double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]

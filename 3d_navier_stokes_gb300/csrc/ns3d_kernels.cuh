@@ -1848,3 +1848,6 @@ __global__ void k_real_pack(const double* __restrict__ u, T* __restrict__ R) {
 }
 
 }  // namespace ns3d
+
+// the tensor-core z pass (z-pass form 2) uses Geo, StepDev and Bits above
+#include "zgemm.cuh"

@@ -39,7 +39,7 @@ ns3d_status load_file(const char* path) {
         if (line[0] == '#' || line[0] == '\n') continue;
         ns3d_tuning t{};
         if (sscanf(line, "%d %d %d %d %f", &t.N, &t.precision, &t.variant, &t.zform, &t.ms_per_step) != 5 ||
-            t.variant < 0 || t.variant >= ns3d::kTileVariants || (t.zform != 0 && t.zform != 1)) {
+            t.variant < 0 || t.variant >= ns3d::kTileVariants || t.zform < 0 || t.zform > 2) {
             st = NS3D_ERR_INVALID;
             continue;
         }
@@ -100,7 +100,8 @@ ns3d_status ns3d_autotune(const ns3d_params* params, int steps, ns3d_tuning* bes
     int count = 0;
     ns3d_status last = NS3D_OK;
     for (int v = 0; v < nvar; ++v) {
-        for (int z = 0; z < 2; ++z) {
+        for (int z = 0; z < 3; ++z) {
+            if (z == 2 && !ns3d::zgemm_size(params->N, params->precision)) continue;
             t_force_variant = v;
             t_force_zform = z;
             ns3d_ctx* c = nullptr;
@@ -154,7 +155,8 @@ ns3d_status ns3d_autotune_ensemble(const ns3d_params* members, int count, int st
         win.ms_per_step = INFINITY;
         ns3d_status last = NS3D_ERR_UNSUPPORTED;
         for (int v = 0; v < nvar; ++v) {
-            for (int z = 0; z < 2; ++z) {
+            for (int z = 0; z < 3; ++z) {
+                if (z == 2 && !ns3d::zgemm_size(g.first.first, g.first.second)) continue;
                 // build this group's engines in shape (v, z); skip shapes the size does not have
                 ns3d_params probe = g.second[0];
                 t_force_variant = v;
@@ -207,7 +209,7 @@ ns3d_status ns3d_tuning_get(int N, int precision, ns3d_tuning* t) {
 }
 
 ns3d_status ns3d_tuning_set(const ns3d_tuning* t) {
-    if (!t || t->variant < 0 || t->variant >= ns3d::kTileVariants || (t->zform != 0 && t->zform != 1) ||
+    if (!t || t->variant < 0 || t->variant >= ns3d::kTileVariants || t->zform < 0 || t->zform > 2 ||
         (t->precision != NS3D_FP32 && t->precision != NS3D_FP64))
         return NS3D_ERR_INVALID;
     std::lock_guard<std::mutex> lk(g_mu);

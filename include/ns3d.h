@@ -257,9 +257,12 @@ ns3d_status ns3d_les_counters(ns3d_ctx* coarse, long* closure_steps, long* fallb
 
 /* ------------------------------------------------------------------------
  * Autotuner. An FP32 engine of a grid size exists in several compiled shapes:
- * tile variants 0..2 (pencils per CTA of the strided x and y FFT passes) and
- * two z-pass forms (0: persistent bulk-copy line kernel, 1: CTA-synchronous
- * pass). ns3d_autotune times every shape of params->N / params->precision on
+ * tile variants 0..6 (pencils per CTA and radix plans of the strided x and y
+ * FFT passes) and up to three z-pass forms (0: persistent bulk-copy line
+ * kernel, 1: CTA-synchronous pass, 2: for N in {16, 32, 48, 64, 96, 128} the
+ * z transforms as dense DFT matrix products on the tensor cores with split-BF16
+ * operands, three terms hi*hi + hi*lo + lo*hi accumulated in FP32, relative
+ * error ~1e-5 per transform). ns3d_autotune times every shape of params->N / params->precision on
  * the configuration *params (SPECTRUM initial condition, k0 = 4, seed 0;
  * 3 warm-up steps, then `steps` timed steps) and keeps the fastest in a
  * process-wide table; ns3d_create and ns3d_ensemble_create then build engines

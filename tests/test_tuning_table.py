@@ -36,7 +36,10 @@ def test_rejects_unknown_shapes(ns3d, tmp_path):
     with pytest.raises(ns3d.NS3DError):
         ns3d.tuning_set(64, 99, 0)     # no such tile variant
     with pytest.raises(ns3d.NS3DError):
-        ns3d.tuning_set(64, 0, 2)      # no such z-pass form
+        ns3d.tuning_set(64, 0, 3)      # no such z-pass form
+    ns3d.tuning_set(64, 0, 2)          # the tensor-core z pass
+    assert shape(ns3d, 64) == (0, 2)
+    ns3d.tuning_clear()
     f = tmp_path / "mixed.txt"
     f.write_text("# N precision variant zform ms\n64 1 2 0 0.5\n96 1 42 0 0.5\n128 1 1 7 0.1\nnot a line\n")
     with pytest.raises(ns3d.NS3DError):
