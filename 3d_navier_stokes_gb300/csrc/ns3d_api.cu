@@ -16,7 +16,8 @@ __global__ void k_dealias_ref_entry(double2* a, int N, int dim);
 
 bool supported_n(int N) {
     switch (N) {
-        case 8: case 16: case 24: case 32: case 48: case 64: case 96: case 128: case 256: case 512: case 1024:
+        case 8: case 16: case 24: case 32: case 48: case 64: case 96: case 128: case 192: case 256: case 384: case 512:
+        case 768: case 1024:
             return true;
         default:
             return false;

@@ -63,6 +63,10 @@ template <> struct Plans<128>  { using A = Plan<128, 16, 16, 8>;     using X = P
 template <> struct Plans<256>  { using A = Plan<256, 16, 16, 16>;    using X = Plan<256, 8, 8, 8, 4>; };
 template <> struct Plans<512>  { using A = Plan<512, 16, 8, 8, 8>;   using X = Plan<512, 8, 8, 8, 8>; };
 template <> struct Plans<1024> { using A = Plan<1024, 16, 16, 16, 4>; using X = Plan<1024, 8, 8, 8, 4, 4>; };
+// sizes with a factor 3 (the reference accepts any even N, utils.c:88-104): 12 elements per thread
+template <> struct Plans<192>  { using A = Plan<192, 12, 4, 4, 12>;    using X = A; };
+template <> struct Plans<384>  { using A = Plan<384, 12, 4, 4, 4, 6>;  using X = A; };
+template <> struct Plans<768>  { using A = Plan<768, 12, 4, 4, 4, 4, 3>; using X = A; };
 
 // Tile width (pencils per CTA along kz) of the strided passes: one 128-byte
 // row segment per pencil row where the thread count allows. Variant V of the

@@ -206,7 +206,30 @@ def test_fp32_vs_fp64_energy(ns3d):
     assert abs(d32 - d64) / d64 < 1e-4
 
 
-@pytest.mark.parametrize("N", [256, 512])
+@pytest.mark.parametrize("N,prec,tol", [(192, "fp64", FP64_TOL), (192, "fp32", FP32_TOL), (384, "fp32", FP32_TOL)])
+def test_rhs_radix3_sizes(ns3d, oracle, N, prec, tol):
+    """Grids with a factor 3 (12 elements per thread, radix-3/6/12 stages): the
+    reference accepts any even N (utils.c:88-104)."""
+    u = dealiased_random(N, N + 2)
+    s = ns3d.Solver(N, precision=prec)
+    got = s.NonlinearRHSBatch(u)
+    s.close()
+    ref = oracle.Oracle(N).rhs(u)
+    assert rel_l2(got, ref) < tol
+
+
+def test_step_radix3_fp64(ns3d, oracle):
+    N = 192
+    s = ns3d.Solver(N, nu=2e-3, dt=1e-3, precision="fp64", forcing="SHELL", force_k=2)
+    o = oracle.Oracle(N, nu=2e-3, dt=1e-3, forcing=oracle.FORCE_SHELL, force_k=2)
+    s.InitialConditions("SPECTRUM", seed=3, k0=4.0)
+    o.ic("SPECTRUM", seed=3, k0=4.0)
+    s.RK4Step(1)
+    o.step(1)
+    assert rel_l2(s.get_state(), o.get_state()) < FP64_TOL
+
+
+@pytest.mark.parametrize("N", [256, 512, 768])
 def test_large_grid_properties(ns3d, N):
     """Size-independent properties at full sizes: the energy budget of one FP32
     step (dE/dt = -eps for unforced flow), divergence-free and dealiased state,
