@@ -46,7 +46,7 @@ EXPORTS = (
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
     "ns3d_les_train", "ns3d_les_dataset_loss", "ns3d_les_weights_host", "ns3d_les_gradients_host",
     "ns3d_les_forward_host", "ns3d_les_attach", "ns3d_les_counters", "ns3d_set_dp_tolerances", "ns3d_dp_stats",
-    "ns3d_set_wait_budget",
+    "ns3d_set_wait_budget", "ns3d_les_set_train_path", "ns3d_les_train_path",
     "ns3d_les_infer_host", "ns3d_les_profile_infer", "ns3d_io_bytes",
     "ns3d_autotune", "ns3d_autotune_ensemble", "ns3d_tuning_get", "ns3d_tuning_set", "ns3d_tuning_clear", "ns3d_tuning_save",
     "ns3d_tuning_load", "ns3d_increment_stats",
@@ -157,6 +157,10 @@ def lib():
         L.ns3d_set_dp_tolerances.restype = I
         L.ns3d_set_dp_tolerances.argtypes = [P, ctypes.c_double, ctypes.c_double]
         L.ns3d_dp_stats.restype = I
+        L.ns3d_les_set_train_path.restype = I
+        L.ns3d_les_set_train_path.argtypes = [P, I]
+        L.ns3d_les_train_path.restype = I
+        L.ns3d_les_train_path.argtypes = [P]
         L.ns3d_set_wait_budget.restype = I
         L.ns3d_set_wait_budget.argtypes = [P, ctypes.c_longlong]
         L.ns3d_dp_stats.argtypes = [P, D, ctypes.POINTER(ctypes.c_long)]
@@ -267,12 +271,13 @@ def autotune(N: int, steps: int = 10, **kw):
     the engines built afterwards. Returns (best, tried) as dicts."""
     p = _params(N, **kw)
     best = Tuning()
-    tried = (Tuning * 16)()
+    cap = 64   # tile variants x z-pass forms
+    tried = (Tuning * cap)()
     n = ctypes.c_int()
-    st = lib().ns3d_autotune(ctypes.byref(p), steps, ctypes.byref(best), tried, 16, ctypes.byref(n))
+    st = lib().ns3d_autotune(ctypes.byref(p), steps, ctypes.byref(best), tried, cap, ctypes.byref(n))
     if st != OK:
         raise NS3DError(st, f"ns3d_autotune(N={N}): {lib().ns3d_status_string(st).decode()}")
-    return best.as_dict(), [tried[i].as_dict() for i in range(n.value)]
+    return best.as_dict(), [tried[i].as_dict() for i in range(min(n.value, cap))]
 
 
 def autotune_ensemble(members, steps: int = 10):
@@ -665,6 +670,14 @@ class LES:
         v = ctypes.c_double()
         self._ck(lib().ns3d_les_dataset_loss(self._h, ctypes.byref(v)))
         return v.value
+
+    def set_train_path(self, path: str):
+        """"tc": tensor cores where compiled (Nc in 16, 32, 64; the default), "fp32": CUDA cores."""
+        self._ck(lib().ns3d_les_set_train_path(self._h, {"tc": 0, "fp32": 1}[path]))
+
+    @property
+    def train_path(self) -> str:
+        return "tc" if lib().ns3d_les_train_path(self._h) == 0 else "fp32"
 
     def weights(self) -> np.ndarray:
         w = np.empty(self.num_params(), np.float32)

@@ -58,6 +58,10 @@ using tc::tmem_relinquish;
 using tc::tmem_wait_ld;
 
 __device__ __forceinline__ float gelu_tc(float x) { return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f)); }
+__device__ __forceinline__ float gelu_grad_tc(float x) {
+    const float cdf = 0.5f * (1.0f + erff(x * 0.70710678118654752f));
+    return cdf + x * 0.39894228040143268f * __expf(-0.5f * x * x);
+}
 
 constexpr int kTcTmemCols = 256;   // two accumulators of up to 96 columns, at 0 and 128
 
@@ -121,7 +125,10 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cout, int cin
 // NO: output channels per dz block (32, or 16 for the output layer);
 // D = 1 << LOGD; input BF16 blocked with KC chunks; OUT_MODE 0: GELU(out + b)
 // as BF16 blocked with 4 chunks, 1: (out + b) * out_scale as FP32
-// [cout][D^3]. 256 threads: thread 0 issues the copies and the MMAs, every
+// [cout][D^3]; training: 2: z = out + b to zbuf (FP32 [32][D^3]) and
+// a = GELU(z) both blocked and channel-major (cm, BF16 [32][D^3]);
+// 3 (the input gradient, weights packed transposed and mirrored by
+// k_pack_tc_t, no bias): d = out * GELU'(zbuf) blocked and channel-major. 256 threads: thread 0 issues the copies and the MMAs, every
 // warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
 // channels [16 (w / 4), 16 (w / 4) + 16).
 constexpr int kTcThreads = 256;
@@ -129,8 +136,10 @@ constexpr int kTcThreads = 256;
 template <int KC, int NO, int LOGD, int OUT_MODE>
 __global__ void __launch_bounds__(kTcThreads, 1)
 k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const float* __restrict__ bias,
-           void* __restrict__ out, int cout, float out_scale, int* __restrict__ status) {
+           void* __restrict__ out, int cout, float out_scale, int* __restrict__ status,
+           float* __restrict__ zbuf = nullptr, __nv_bfloat16* __restrict__ cm = nullptr) {
     static_assert(KC % 2 == 0 && (NO == 16 || NO == 32), "tile shape");
+    static_assert(OUT_MODE < 2 || NO == 32, "the training modes write 32 channels");
     constexpr int D = 1 << LOGD, R = 128 / D, rows = R + 2, ZG = D / 8, NB = 3 * NO;
     static_assert(R >= 1 && R <= D, "grid size");
     constexpr uint32_t b_bytes = tc_b_bytes(KC, NO), a_bytes = tc_a_bytes(KC, D);
@@ -277,6 +286,26 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
                                    pack_bf16x2(gelu_tc(v[q * 8 + 2]), gelu_tc(v[q * 8 + 3])),
                                    pack_bf16x2(gelu_tc(v[q * 8 + 4]), gelu_tc(v[q * 8 + 5])),
                                    pack_bf16x2(gelu_tc(v[q * 8 + 6]), gelu_tc(v[q * 8 + 7])));
+            } else if constexpr (OUT_MODE == 2 || OUT_MODE == 3) {
+                const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
+                float o[16];
+#pragma unroll
+                for (int j = 0; j < 16; ++j) {
+                    const long long qi = (long long)(16 * half + j) * D3 + p;
+                    if constexpr (OUT_MODE == 2) {
+                        zbuf[qi] = v[j];
+                        o[j] = gelu_tc(v[j]);
+                    } else {
+                        o[j] = v[j] * gelu_grad_tc(zbuf[qi]);
+                    }
+                    cm[qi] = __float2bfloat16_rn(o[j]);
+                }
+                uint4* dst = reinterpret_cast<uint4*>(out);
+#pragma unroll
+                for (int q = 0; q < 2; ++q)
+                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] =
+                        make_uint4(pack_bf16x2(o[q * 8 + 0], o[q * 8 + 1]), pack_bf16x2(o[q * 8 + 2], o[q * 8 + 3]),
+                                   pack_bf16x2(o[q * 8 + 4], o[q * 8 + 5]), pack_bf16x2(o[q * 8 + 6], o[q * 8 + 7]));
             } else {
                 float* dst = reinterpret_cast<float*>(out);
                 const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
@@ -302,6 +331,267 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, kTcTmemCols);
+}
+
+
+// ------------------------------------------------------------------ training
+// Tensor-core training of the network (BF16 operands, FP32 accumulation,
+// FP32 master weights and Adam outside). Notation for layer L: z_L = conv(a_{L-1},
+// W_L) + b_L, a_L = GELU(z_L) (L = 1..3), y = z_4; the loss gradient
+// d_4 = dloss/dy, d_L = conv^T(d_{L+1}, W_{L+1}) * GELU'(z_L),
+// dW_L[co][ci][t] = sum_p d_L[co][p] a_{L-1}[ci][p + off_t], db_L = sum_p d_L.
+// The forward convolutions (OUT_MODE 2) and the input gradients (OUT_MODE 3,
+// a convolution with the weights transposed and mirrored) run on k_conv3_tc;
+// the weight gradients on k_wgrad_tc, whose operands are "channel-major"
+// BF16 copies [channel][x][y][z] of the activations and gradients that those
+// kernels also write.
+
+// B operand of the input-gradient convolution of a layer with weights
+// W[cout][cin][27]: the transposed, mirrored kernel W'[ci][co][t] =
+// W[co][ci][26 - t] (input channels co in KC chunks, output channels ci < NO),
+// in k_pack_tc's shared-memory order
+__global__ void k_pack_tc_t(const __nv_bfloat16* __restrict__ w, int cout, int cin, int KC, int NO,
+                            __nv_bfloat16* __restrict__ dst) {
+    const int NG = 3 * NO / 8;
+    const int n_all = 9 * NG * KC * 64;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_all; q += gridDim.x * blockDim.x) {
+        const int j = q % 8;
+        int r = q / 8;
+        const int n8 = r % 8;
+        r /= 8;
+        const int kc = r % KC;
+        r /= KC;
+        const int ng = r % NG;
+        const int t9 = r / NG;
+        const int n = ng * 8 + n8, dz = n / NO, o = n % NO, i = kc * 8 + j;
+        const int t = t9 * 3 + dz;
+        dst[q] = (o < cin && i < cout) ? w[((long long)i * cin + o) * 27 + (26 - t)] : __float2bfloat16(0.0f);
+    }
+}
+
+// FP32 velocity [3][D^3] x in_scale -> channel-major BF16 [8][D^3] (channels 3..7 zero)
+template <int LOGD>
+__global__ void k_to_cm(const float* __restrict__ u, float in_scale, __nv_bfloat16* __restrict__ dst) {
+    constexpr long long D3 = 1ll << (3 * LOGD);
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) dst[c * D3 + p] = __float2bfloat16_rn(c < 3 ? u[c * D3 + p] * in_scale : 0.0f);
+    }
+}
+
+// the output gradient d_4 (FP32 [6][D^3]) -> blocked BF16 with 2 chunks (16
+// channels, 6 used) and channel-major BF16 [16][D^3] (channels 6..15 zero)
+template <int LOGD>
+__global__ void k_grad_pack(const float* __restrict__ g, uint4* __restrict__ blk, __nv_bfloat16* __restrict__ cm) {
+    constexpr int D = 1 << LOGD;
+    constexpr long long D3 = (long long)D * D * D;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x) {
+        const int z = (int)(p & (D - 1)), y = (int)((p >> LOGD) & (D - 1)), x = (int)(p >> (2 * LOGD));
+        float v[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) {
+            v[c] = c < 6 ? g[c * D3 + p] : 0.0f;
+            cm[c * D3 + p] = __float2bfloat16_rn(v[c]);
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q)
+            blk[blk_index<LOGD, 2>(x, y, z, q)] =
+                make_uint4(pack_bf16x2(v[q * 8 + 0], v[q * 8 + 1]), pack_bf16x2(v[q * 8 + 2], v[q * 8 + 3]),
+                           pack_bf16x2(v[q * 8 + 4], v[q * 8 + 5]), pack_bf16x2(v[q * 8 + 6], v[q * 8 + 7]));
+    }
+}
+
+// per-channel sums (bias gradients), one CTA per channel, fixed order
+template <typename T>
+__global__ void k_chan_sum(const T* __restrict__ x, long long D3, float* __restrict__ out) {
+    __shared__ float red[256];
+    const T* xc = x + (long long)blockIdx.x * D3;
+    float s = 0.0f;
+    for (long long p = threadIdx.x; p < D3; p += blockDim.x) s += (float)xc[p];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
+}
+
+__host__ __device__ constexpr int tc_pow2(int v) {
+    int p = 32;
+    while (p < v) p <<= 1;
+    return p;
+}
+// byte offset of the 16-byte chunk (row r, K elements 8 k8 ..) of a canonical K-major operand with K columns
+__host__ __device__ constexpr uint32_t tc_chunk(int r, int k8, int K) {
+    return (uint32_t)(((r >> 3) * (K >> 3) + k8) * 128 + (r & 7) * 16);
+}
+
+// Weight gradient on the tensor cores. For one z line (x, y) of D points, the
+// GEMM D[(t, ci)][(j, co)] += sum_z a[ci][x + dx_t][y + dy_t][z] d[co][x][y][z - (j - 1)]
+// accumulates dW[co][ci][(t, j)] (t = the (dx, dy) tap, j = dz + 1: the dz taps
+// are the N dimension through z-shifted copies of d). M = 128 rows: TG = 128 / CI
+// (dx, dy) taps of CI channels per tap group, ceil(9 / TG) groups; N = 3 NB;
+// K = the D points of the line, both operands K-major (channel-major sources,
+// 8 consecutive points per 16-byte row). Persistent CTAs walk the D^2 lines,
+// staging line i + 1 (all threads) while the MMAs of line i run (thread 0,
+// double-buffered, bounded waits); each CTA writes its FP32 partial sums
+// [group][128][3 NB] to part, reduced in a fixed order by k_wgrad_reduce.
+template <int CI, int NB, int LOGD>
+struct WgGeo {
+    static constexpr int D = 1 << LOGD, TG = 128 / CI, NGRP = (9 + TG - 1) / TG, NN = 3 * NB, K8 = D / 8;
+    static constexpr uint32_t A_BYTES = 128u * D * 2, B_BYTES = (uint32_t)NN * D * 2;
+    static constexpr uint32_t STAGE = NGRP * A_BYTES + B_BYTES;
+    static constexpr int TCOLS = tc_pow2(NGRP * NN);
+    static constexpr uint32_t need = 2 * STAGE + 64;
+    // at least enough shared memory that no more CTAs share an SM than its 512 tensor-memory columns hold
+    static constexpr uint32_t floor_bytes = 233472u / (512u / (uint32_t)TCOLS + 1u) - 1024u + 16u;
+    static constexpr uint32_t SMEM = need > floor_bytes ? need : floor_bytes;
+    static constexpr int PART = NGRP * 128 * NN;   // floats of one CTA's partial sums
+};
+
+template <int CI, int NB, int LOGD>
+__global__ void __launch_bounds__(kTcThreads, 1)
+k_wgrad_tc(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict__ d, float* __restrict__ part,
+           int* __restrict__ status) {
+    using WG = WgGeo<CI, NB, LOGD>;
+    constexpr int D = WG::D, TG = WG::TG, NGRP = WG::NGRP, NN = WG::NN, K8 = WG::K8;
+    constexpr long long D3 = (long long)D * D * D;
+    constexpr int nlines = D * D;
+    constexpr uint32_t SBO = K8 * 128;
+    constexpr uint32_t idesc = idesc_bf16(128, NN);
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* done = reinterpret_cast<uint64_t*>(smem + 2 * WG::STAGE);
+    uint32_t* holder = reinterpret_cast<uint32_t*>(done + 2);
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (tid == 0) {
+        mbar_init(&done[0], 1);
+        mbar_init(&done[1], 1);
+        fence_barrier_init();
+        s_ok = 1;
+    }
+    if (warp == 0) {
+        tmem_alloc(holder, WG::TCOLS);
+        tmem_relinquish();
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = *holder;
+    const uint32_t s_u = smem_u32(smem);
+    uint32_t ph[2] = {0u, 0u};
+    bool pend[2] = {false, false};
+    bool ok = true;
+    int it = 0, last = 0;
+    for (int line = blockIdx.x; line < nlines && s_ok; line += gridDim.x, ++it) {
+        const int b = it & 1;
+        if (tid == 0 && pend[b]) {
+            if (ok) ok = mbar_wait(&done[b], ph[b]);
+            if (ok) {
+                ph[b] ^= 1u;
+                pend[b] = false;
+            } else {
+                s_ok = 0;
+                atomicExch(status, kStatusTimeout);
+            }
+        }
+        __syncthreads();
+        if (!s_ok) break;
+        const int x = line >> LOGD, y = line & (D - 1);
+        unsigned char* sa = smem + b * WG::STAGE;
+        unsigned char* sb = sa + NGRP * WG::A_BYTES;
+        for (int q = tid; q < NGRP * 128 * K8; q += kTcThreads) {
+            const int g = q / (128 * K8), rem = q % (128 * K8), r = rem / K8, k8 = rem % K8;
+            const int t9 = g * TG + r / CI, ci = r % CI;
+            uint4 v = make_uint4(0u, 0u, 0u, 0u);
+            if (t9 < 9) {
+                const int gx = (x + t9 / 3 - 1) & (D - 1), gy = (y + t9 % 3 - 1) & (D - 1);
+                v = *reinterpret_cast<const uint4*>(a + ci * D3 + (((long long)gx << LOGD) + gy) * D + k8 * 8);
+            }
+            *reinterpret_cast<uint4*>(sa + g * WG::A_BYTES + tc_chunk(r, k8, D)) = v;
+        }
+        for (int q = tid; q < NN * K8; q += kTcThreads) {
+            const int n = q / K8, k8 = q % K8, j = n / NB, co = n % NB;
+            const unsigned short* src =
+                reinterpret_cast<const unsigned short*>(d + co * D3 + (((long long)x << LOGD) + y) * D);
+            uint32_t w4[4];
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const int z0 = k8 * 8 + 2 * e;
+                const uint32_t lo = src[(z0 - (j - 1)) & (D - 1)], hi = src[(z0 + 1 - (j - 1)) & (D - 1)];
+                w4[e] = lo | (hi << 16);
+            }
+            *reinterpret_cast<uint4*>(sb + tc_chunk(n, k8, D)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+        }
+        fence_proxy_async_smem();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+            const uint32_t a0 = s_u + b * WG::STAGE, b0 = a0 + NGRP * WG::A_BYTES;
+#pragma unroll 1
+            for (int g = 0; g < NGRP; ++g)
+#pragma unroll 1
+                for (int ks = 0; ks < D / 16; ++ks)
+                    mma_bf16(tmem + g * NN, smem_desc(a0 + g * WG::A_BYTES + ks * 256, 128, SBO),
+                             smem_desc(b0 + ks * 256, 128, SBO), idesc, (it > 0 || ks > 0) ? 1u : 0u);
+            mma_commit(&done[b]);
+            pend[b] = true;
+            last = b;
+        }
+    }
+    if (tid == 0 && s_ok) {
+        if (ok) ok = mbar_wait(&done[last], ph[last]);
+        if (ok) {
+            ph[last] ^= 1u;
+            pend[last] = false;
+        } else {
+            s_ok = 0;
+            atomicExch(status, kStatusTimeout);
+        }
+    }
+    __syncthreads();
+    if (s_ok) {
+        tc_fence_after();
+        const int quarter = warp & 3, hh = warp >> 2;
+        const int row = quarter * 32 + lane;
+        float* dst = part + (long long)blockIdx.x * WG::PART;
+#pragma unroll 1
+        for (int i = hh; i < NGRP * (NN / 16); i += 2) {
+            const int g = i / (NN / 16), c = i % (NN / 16);
+            uint32_t r[16];
+            tmem_ld16(tmem + ((uint32_t)(quarter * 32) << 16) + g * NN + c * 16, r);
+            tmem_wait_ld(r);
+            float4* o = reinterpret_cast<float4*>(dst + ((long long)g * 128 + row) * NN + c * 16);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                o[j] = make_float4(__uint_as_float(r[4 * j]), __uint_as_float(r[4 * j + 1]), __uint_as_float(r[4 * j + 2]),
+                                   __uint_as_float(r[4 * j + 3]));
+        }
+    }
+    if (tid == 0) {
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+            if (pend[b]) (void)mbar_wait(&done[b], ph[b]);
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0) tmem_dealloc(tmem, WG::TCOLS);
+}
+
+// sum of the CTAs' partials in CTA order, scattered to dW[co][ci][27]
+__global__ void k_wgrad_reduce(const float* __restrict__ part, int nparts, int CI, int NB, int ngrp, int cin,
+                               int cout, float* __restrict__ dw) {
+    const int NN = 3 * NB, TG = 128 / CI, width = ngrp * 128 * NN;
+    const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e >= width) return;
+    const int g = e / (128 * NN), r = (e / NN) % 128, n = e % NN;
+    const int t9 = g * TG + r / CI, ci = r % CI, j = n / NB, co = n % NB;
+    if (t9 >= 9 || ci >= cin || co >= cout) return;
+    float s = 0.0f;
+    for (int q = 0; q < nparts; ++q) s += part[(long long)q * width + e];
+    dw[((long long)co * cin + ci) * 27 + t9 * 3 + j] = s;
 }
 
 }  // namespace cnn

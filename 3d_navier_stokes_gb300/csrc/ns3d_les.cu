@@ -86,6 +86,10 @@ constexpr int NPART = 256;
 // (KC, NO) = (2, 32), (4, 32), (4, 32), (4, 16); 9 x 3 NO x 8 KC each
 constexpr int kTcW1 = 9 * 96 * 2 * 8, kTcW2 = 9 * 96 * 4 * 8, kTcW4 = 9 * 48 * 4 * 8;
 constexpr int oT1 = 0, oT2 = oT1 + kTcW1, oT3 = oT2 + kTcW2, oT4 = oT3 + kTcW2, kTcWTotal = oT4 + kTcW4;
+// packed B operands of the input-gradient convolutions (transposed, mirrored
+// weights): layer 4 (6 -> 32, KC 2), layers 3 and 2 (32 -> 32, KC 4)
+constexpr int kTcT4 = 9 * 96 * 2 * 8, kTcT3 = 9 * 96 * 4 * 8;
+constexpr int oU4 = 0, oU3 = oU4 + kTcT4, oU2 = oU3 + kTcT3, kTcTTotal = oU2 + kTcT3;
 
 unsigned long long sm64(unsigned long long& s) {
     unsigned long long z = (s += 0x9E3779B97F4A7C15ull);
@@ -109,6 +113,16 @@ struct ns3d_les : public ns3d::LesHook {
     __nv_bfloat16* wtc = nullptr;                        // packed B operands
     __nv_bfloat16 *act0 = nullptr, *act1 = nullptr, *act2 = nullptr, *act3 = nullptr;   // blocked BF16 activations
     int* dstat = nullptr;                                // device status word
+    // tensor-core training (Nc in {16, 32, 64}): transposed weight packs,
+    // channel-major BF16 activations a0 (8 channels) .. a3 and gradients d1 .. d4
+    // (d4: 16 channels), the weight-gradient partial sums, a zero bias
+    __nv_bfloat16* wtc_t = nullptr;
+    __nv_bfloat16 *a0cm = nullptr, *a1cm = nullptr, *a2cm = nullptr, *a3cm = nullptr;
+    __nv_bfloat16 *d1cm = nullptr, *d2cm = nullptr, *d3cm = nullptr, *d4cm = nullptr;
+    float* wpart = nullptr;
+    float* zeros = nullptr;
+    int wg_grid = 0;
+    int train_path = 0;                                  // 0: tensor cores where compiled, 1: FP32 CUDA cores
     int tc_grid[3] = {0, 0, 0};                          // CTAs of the three kernel shapes
     double s_in = 1.0, s_out = 1.0;
     bool scales_set = false;
@@ -149,6 +163,89 @@ struct ns3d_les : public ns3d::LesHook {
     }
 
     bool tc() const { return ns3d::cnn::tc_grid_ok(Nc) && wtc != nullptr; }
+    bool tc_train() const { return tc() && wtc_t != nullptr && train_path == 0; }
+
+    // B operands of the input-gradient convolutions from the current BF16 weights
+    void pack_tc_t(cudaStream_t s) {
+        if (!wtc_t) return;
+        using ns3d::cnn::k_pack_tc_t;
+        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW4, 6, C, 2, 32, wtc_t + oU4);
+        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW3, C, C, 4, 32, wtc_t + oU3);
+        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW2, C, C, 4, 32, wtc_t + oU2);
+    }
+
+    // dW of one layer on the tensor cores, reduced into g + off (cin x cout x 27)
+    template <int CI, int NB, int LOGD>
+    void wgrad_tc(const __nv_bfloat16* a, const __nv_bfloat16* d, int cin, int cout, int off, cudaStream_t s) {
+        using namespace ns3d::cnn;
+        using WG = WgGeo<CI, NB, LOGD>;
+        const int grid = wg_grid < WG::D * WG::D ? wg_grid : WG::D * WG::D;
+        k_wgrad_tc<CI, NB, LOGD><<<grid, kTcThreads, WG::SMEM, s>>>(a, d, wpart, dstat);
+        k_wgrad_reduce<<<(WG::PART + 255) / 256, 256, 0, s>>>(wpart, grid, CI, NB, WG::NGRP, cin, cout, g + off);
+    }
+
+    // loss and gradients of one sample on the tensor cores (BF16 operands, FP32
+    // accumulation): forward with the pre-activations kept, then per layer the
+    // bias and weight gradients and the input gradient
+    template <int LOGD>
+    double fwd_bwd_tc_d(const float* u, const float* t, cudaStream_t s) {
+        using namespace ns3d::cnn;
+        constexpr int D = 1 << LOGD;
+        const float is = (float)(1.0 / s_in);
+        const uint4* W = reinterpret_cast<const uint4*>(wtc);
+        const uint4* WT = reinterpret_cast<const uint4*>(wtc_t);
+        uint4* b0 = reinterpret_cast<uint4*>(act0);
+        uint4* b1 = reinterpret_cast<uint4*>(act1);
+        uint4* b2 = reinterpret_cast<uint4*>(act2);
+        uint4* b3 = reinterpret_cast<uint4*>(act3);
+        const unsigned eg = (unsigned)((D3 + 255) / 256);
+        k_to_blocked<LOGD><<<eg, 256, 0, s>>>(u, is, b0);
+        k_to_cm<LOGD><<<eg, 256, 0, s>>>(u, is, a0cm);
+        k_conv3_tc<2, 32, LOGD, 2><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+            b0, W + oT1 / 8, w + ob1, b1, C, 1.f, dstat, z1, a1cm);
+        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            b1, W + oT2 / 8, w + ob2, b2, C, 1.f, dstat, z2, a2cm);
+        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            b2, W + oT3 / 8, w + ob3, b3, C, 1.f, dstat, z3, a3cm);
+        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kTcThreads, tc_smem_bytes(4, 16, D), s>>>(
+            b3, W + oT4 / 8, w + ob4, y, 6, 1.f, dstat);
+        k_mse<<<NPART, 256, 0, s>>>(y, t, (float)(1.0 / s_out), gy, 6 * D3, part);
+        // layer 4: d4 = dloss/dy (blocked into b0, which the forward no longer needs)
+        k_grad_pack<LOGD><<<eg, 256, 0, s>>>(gy, b0, d4cm);
+        k_chan_sum<float><<<6, 256, 0, s>>>(gy, D3, g + ob4);
+        wgrad_tc<32, 16, LOGD>(a3cm, d4cm, C, 6, oW4, s);
+        k_conv3_tc<2, 32, LOGD, 3><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+            b0, WT + oU4 / 8, zeros, b3, C, 1.f, dstat, z3, d3cm);
+        // layer 3
+        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d3cm, D3, g + ob3);
+        wgrad_tc<32, 32, LOGD>(a2cm, d3cm, C, C, oW3, s);
+        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            b3, WT + oU3 / 8, zeros, b2, C, 1.f, dstat, z2, d2cm);
+        // layer 2
+        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d2cm, D3, g + ob2);
+        wgrad_tc<32, 32, LOGD>(a1cm, d2cm, C, C, oW2, s);
+        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+            b2, WT + oU2 / 8, zeros, b1, C, 1.f, dstat, z1, d1cm);
+        // layer 1
+        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d1cm, D3, g + ob1);
+        wgrad_tc<8, 32, LOGD>(a0cm, d1cm, 3, C, oW1, s);
+        cudaMemcpyAsync(part_host, part, sizeof(double) * NPART, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(part_host + NPART, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
+        cudaStreamSynchronize(s);
+        if (*reinterpret_cast<const int*>(part_host + NPART) != 0) return NAN;   // a bounded wait gave up
+        double l = 0.0;
+        for (int i = 0; i < NPART; ++i) l += part_host[i];
+        return l / (double)(6 * D3);
+    }
+    double fwd_bwd_tc(const float* u, const float* t, cudaStream_t s) {
+        if (Nc == 16) return fwd_bwd_tc_d<4>(u, t, s);
+        if (Nc == 32) return fwd_bwd_tc_d<5>(u, t, s);
+        return fwd_bwd_tc_d<6>(u, t, s);
+    }
+    // the training path's loss and gradients (tensor cores where compiled and selected)
+    double fwd_bwd_train(const float* u, const float* t, cudaStream_t s) {
+        return tc_train() ? fwd_bwd_tc(u, t, s) : fwd_bwd(u, t, s);
+    }
 
     // B operands of the tensor-core layers from the current BF16 weights
     void pack_tc(cudaStream_t s) {
@@ -197,7 +294,8 @@ struct ns3d_les : public ns3d::LesHook {
         for (void* q : {(void*)data_u, (void*)data_t, (void*)w, (void*)g, (void*)m, (void*)v, (void*)wb, (void*)z1,
                         (void*)z2, (void*)z3, (void*)y, (void*)gy, (void*)gz3, (void*)gz2, (void*)gz1, (void*)io_u,
                         (void*)io_t, (void*)part, (void*)wtc, (void*)act0, (void*)act1, (void*)act2, (void*)act3,
-                        (void*)dstat})
+                        (void*)dstat, (void*)wtc_t, (void*)a0cm, (void*)a1cm, (void*)a2cm, (void*)a3cm, (void*)d1cm,
+                        (void*)d2cm, (void*)d3cm, (void*)d4cm, (void*)wpart, (void*)zeros})
             if (q) cudaFree(q);
         if (part_host) cudaFreeHost(part_host);
         if (stream) cudaStreamDestroy(stream);
@@ -220,6 +318,21 @@ static ns3d_status les_tc_setup_d(ns3d_les* l, int nsm) {
             return NS3D_ERR_CUDA;
         l->tc_grid[k] = per * nsm < ntiles ? per * nsm : ntiles;
     }
+    // training: the same layer shapes in the training modes, and the weight-gradient kernels
+    const void* tfns[4] = {(const void*)k_conv3_tc<2, 32, LOGD, 2>, (const void*)k_conv3_tc<4, 32, LOGD, 2>,
+                           (const void*)k_conv3_tc<2, 32, LOGD, 3>, (const void*)k_conv3_tc<4, 32, LOGD, 3>};
+    const uint32_t tsm[4] = {tc_smem_bytes(2, 32, D), tc_smem_bytes(4, 32, D), tc_smem_bytes(2, 32, D),
+                             tc_smem_bytes(4, 32, D)};
+    for (int k = 0; k < 4; ++k)
+        if (cudaFuncSetAttribute(tfns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tsm[k]) != cudaSuccess)
+            return NS3D_ERR_CUDA;
+    const void* wfns[3] = {(const void*)k_wgrad_tc<32, 16, LOGD>, (const void*)k_wgrad_tc<32, 32, LOGD>,
+                           (const void*)k_wgrad_tc<8, 32, LOGD>};
+    const uint32_t wsm[3] = {WgGeo<32, 16, LOGD>::SMEM, WgGeo<32, 32, LOGD>::SMEM, WgGeo<8, 32, LOGD>::SMEM};
+    for (int k = 0; k < 3; ++k)
+        if (cudaFuncSetAttribute(wfns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)wsm[k]) != cudaSuccess)
+            return NS3D_ERR_CUDA;
+    l->wg_grid = nsm;
     return NS3D_OK;
 }
 
@@ -266,7 +379,7 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
         cudaMalloc(&l->gz2, f * C * l->D3) != cudaSuccess || cudaMalloc(&l->gz1, f * C * l->D3) != cudaSuccess ||
         cudaMalloc(&l->io_u, f * 3 * l->D3) != cudaSuccess || cudaMalloc(&l->io_t, f * 6 * l->D3) != cudaSuccess ||
         cudaMalloc(&l->part, sizeof(double) * NPART) != cudaSuccess ||
-        cudaMallocHost(&l->part_host, sizeof(double) * NPART) != cudaSuccess ||
+        cudaMallocHost(&l->part_host, sizeof(double) * (NPART + 1)) != cudaSuccess ||
         (capacity > 0 && (cudaMalloc(&l->data_u, f * 3 * l->D3 * capacity) != cudaSuccess ||
                           cudaMalloc(&l->data_t, f * 6 * l->D3 * capacity) != cudaSuccess))) {
         delete l;
@@ -295,15 +408,26 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
     }
     if (ns3d::cnn::tc_grid_ok(Nc)) {
         const size_t a = sizeof(__nv_bfloat16) * C * (size_t)l->D3;
+        int nsm = 0, dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (cudaMalloc(&l->wtc, sizeof(__nv_bfloat16) * kTcWTotal) != cudaSuccess || cudaMalloc(&l->act0, a / 2) != cudaSuccess ||
             cudaMalloc(&l->act1, a) != cudaSuccess ||
             cudaMalloc(&l->act2, a) != cudaSuccess || cudaMalloc(&l->act3, a) != cudaSuccess ||
+            cudaMalloc(&l->wtc_t, sizeof(__nv_bfloat16) * kTcTTotal) != cudaSuccess ||
+            cudaMalloc(&l->a0cm, a / 4) != cudaSuccess || cudaMalloc(&l->a1cm, a) != cudaSuccess ||
+            cudaMalloc(&l->a2cm, a) != cudaSuccess || cudaMalloc(&l->a3cm, a) != cudaSuccess ||
+            cudaMalloc(&l->d1cm, a) != cudaSuccess || cudaMalloc(&l->d2cm, a) != cudaSuccess ||
+            cudaMalloc(&l->d3cm, a) != cudaSuccess || cudaMalloc(&l->d4cm, a / 2) != cudaSuccess ||
+            cudaMalloc(&l->wpart, sizeof(float) * 3 * 128 * 96 * (size_t)(nsm > 0 ? nsm : 1)) != cudaSuccess ||
+            cudaMalloc(&l->zeros, sizeof(float) * C) != cudaSuccess || cudaMemset(l->zeros, 0, sizeof(float) * C) != cudaSuccess ||
             les_tc_setup(l) != NS3D_OK) {
             delete l;
             cudaGetLastError();
             return NS3D_ERR_NOMEM;
         }
         l->pack_tc(l->stream);
+        l->pack_tc_t(l->stream);
     }
     if (cudaStreamSynchronize(l->stream) != cudaSuccess) {
         delete l;
@@ -402,13 +526,22 @@ ns3d_status ns3d_les_train(ns3d_les* l, int iterations, double lr, double* mean_
     int nacc = 0;
     for (int it = 0; it < iterations; ++it) {
         const int smp = (int)(sm64(l->rng) % (unsigned long long)l->count);
-        const double loss = l->fwd_bwd(l->data_u + 3 * l->D3 * smp, l->data_t + 6 * l->D3 * smp, l->stream);
-        if (!isfinite(loss)) return les_fail(l, NS3D_ERR_NUMERIC, "training loss is not finite");
+        const double loss = l->fwd_bwd_train(l->data_u + 3 * l->D3 * smp, l->data_t + 6 * l->D3 * smp, l->stream);
+        if (!isfinite(loss)) {
+            int st = 0;
+            cudaMemcpy(&st, l->dstat, sizeof(int), cudaMemcpyDeviceToHost);
+            if (st != 0) return les_fail(l, NS3D_ERR_TIMEOUT, "a bounded wait in a tensor-core training kernel gave up");
+            return les_fail(l, NS3D_ERR_NUMERIC, "training loss is not finite");
+        }
         l->adam_t++;
         const float b1 = 0.9f, b2 = 0.999f;
         const float c1 = 1.0f - powf(b1, (float)l->adam_t), c2 = 1.0f - powf(b2, (float)l->adam_t);
         ns3d::cnn::k_adam<<<(NPARAM + 255) / 256, 256, 0, l->stream>>>(l->w, l->wb, l->g, l->m, l->v, NPARAM,
                                                                       (float)lr, b1, b2, 1e-8f, c1, c2);
+        if (l->tc_train()) {   // the next sample's tensor-core layers read the updated weights
+            l->pack_tc(l->stream);
+            l->pack_tc_t(l->stream);
+        }
         if (it >= iterations - iterations / 10 - 1) {
             acc += loss;
             nacc++;
@@ -456,11 +589,19 @@ ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* ta
     if (!l || !u || !tau) return NS3D_ERR_INVALID;
     LES_CK(cudaMemcpy(l->io_u, u, sizeof(float) * 3 * l->D3, cudaMemcpyHostToDevice));
     LES_CK(cudaMemcpy(l->io_t, tau, sizeof(float) * 6 * l->D3, cudaMemcpyHostToDevice));
-    const double ls = l->fwd_bwd(l->io_u, l->io_t, l->stream);
+    const double ls = l->fwd_bwd_train(l->io_u, l->io_t, l->stream);
     if (loss) *loss = ls;
     if (grads) LES_CK(cudaMemcpy(grads, l->g, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost));
     return NS3D_OK;
 }
+
+ns3d_status ns3d_les_set_train_path(ns3d_les* l, int path) {
+    if (!l || (path != 0 && path != 1)) return NS3D_ERR_INVALID;
+    l->train_path = path;
+    return NS3D_OK;
+}
+
+int ns3d_les_train_path(const ns3d_les* l) { return l ? (l->tc_train() ? 0 : 1) : -1; }
 
 ns3d_status ns3d_les_forward_host(ns3d_les* l, const float* u, float* tau) {
     if (!l || !u || !tau) return NS3D_ERR_INVALID;

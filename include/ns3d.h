@@ -77,7 +77,10 @@ typedef struct {
 typedef struct ns3d_ctx ns3d_ctx;
 
 const char* ns3d_status_string(ns3d_status s);
-/* 1 when a compiled FFT plan exists for grid size N, else 0. */
+/* 1 when a compiled FFT plan exists for grid size N, else 0: N = 8, 16, 24,
+ * 32, 48, 64, 96, 128, 192, 256, 384, 512, 768, 1024 (cubic grids; the
+ * reference's GetCMLArgs accepts any even N > 2, utils.c:88-104, and other
+ * sizes return NS3D_ERR_UNSUPPORTED from ns3d_create). */
 int ns3d_supported_size(int N);
 /* Length of the spectrum arrays, sys_vars->n_spect (solver.c:1384). */
 int ns3d_n_spect(int N);
@@ -235,12 +238,21 @@ ns3d_status ns3d_les_filtered_velocity_host(ns3d_les* l, ns3d_ctx* fine, double*
 /* input scale s_in and output scale s_out (default: RMS of ubar over the dataset, its square) */
 ns3d_status ns3d_les_set_scales(ns3d_les* l, double s_in, double s_out);
 ns3d_status ns3d_les_get_scales(ns3d_les* l, double* s_in, double* s_out);
-/* Adam over random dataset samples; mean_loss = mean MSE of the last 10% of iterations */
+/* Adam over random dataset samples; mean_loss = mean MSE of the last 10% of iterations.
+ * For Nc in {16, 32, 64} the forward, input-gradient and weight-gradient
+ * convolutions run on the tensor cores (tcgen05, BF16 operands, FP32
+ * accumulation; FP32 master weights for Adam); elsewhere, or after
+ * ns3d_les_set_train_path(l, 1), on FP32 CUDA cores. */
 ns3d_status ns3d_les_train(ns3d_les* l, int iterations, double lr, double* mean_loss);
+/* training path: 0 = tensor cores where compiled (default), 1 = FP32 CUDA cores;
+ * ns3d_les_train_path returns the path training will take (0 or 1) */
+ns3d_status ns3d_les_set_train_path(ns3d_les* l, int path);
+int ns3d_les_train_path(const ns3d_les* l);
 ns3d_status ns3d_les_dataset_loss(ns3d_les* l, double* mean_loss);
 /* FP32 master weights (ns3d_les_num_params floats), get (set = 0) or set */
 ns3d_status ns3d_les_weights_host(ns3d_les* l, float* w, int set);
-/* loss and weight gradients for one sample (u [3][Nc^3], tau [6][Nc^3] host floats) */
+/* loss and weight gradients for one sample (u [3][Nc^3], tau [6][Nc^3] host floats),
+ * through the training path */
 ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* tau, double* loss, float* grads);
 /* tau = network(u) in physical units, the FP32 training network (FP32 activations) */
 ns3d_status ns3d_les_forward_host(ns3d_les* l, const float* u, float* tau);
@@ -268,7 +280,8 @@ ns3d_status ns3d_les_counters(ns3d_ctx* coarse, long* closure_steps, long* fallb
  * process-wide table; ns3d_create and ns3d_ensemble_create then build engines
  * of that (N, precision) in the chosen shape. The table can be saved to and
  * loaded from a text file; the environment variable NS3D_TUNING_FILE names a
- * file loaded before the first engine is built. */
+ * file loaded before the first engine is built. *n_tried counts every shape
+ * timed; tried[] receives the first max_tried of them. */
 typedef struct {
     int   N;
     int   precision;    /* ns3d_precision                          */

@@ -37,7 +37,8 @@ def test_tile_variants_are_bit_identical(ns3d, N):
 def test_autotune_picks_fastest_and_persists(ns3d, tmp_path):
     ns3d.tuning_clear()
     best, tried = ns3d.autotune(64, steps=10, precision="fp32", nu=0.005, dt=1e-3)
-    assert len(tried) == 14   # 7 variants x 2 z-pass forms at 64^3
+    assert len(tried) == 21   # 7 variants x 3 z-pass forms at 64^3 (form 2: the tensor-core z pass)
+    assert {t["zform"] for t in tried} == {0, 1, 2}
     assert best["ms_per_step"] == min(t["ms_per_step"] for t in tried)
     assert ns3d.tuning(64) == best
     f = tmp_path / "tune.txt"
@@ -63,7 +64,7 @@ def test_autotune_picks_fastest_and_persists(ns3d, tmp_path):
 
 def test_fp64_has_one_shape(ns3d):
     best, tried = ns3d.autotune(32, steps=3, precision="fp64", nu=0.01, dt=1e-3)
-    assert len(tried) == 1 and best["zform"] == 1
+    assert len(tried) == 1 and best["zform"] == 1   # no line kernel and no tensor-core z pass in FP64
     ns3d.tuning_clear()
 
 

@@ -58,6 +58,42 @@ def test_cnn_gradients_and_forward_vs_cpu(ns3d):
     les.close()
 
 
+BLOCKS = [("W1", C * 3 * 27), ("b1", C), ("W2", C * C * 27), ("b2", C), ("W3", C * C * 27), ("b3", C),
+          ("W4", 6 * C * 27), ("b4", 6)]
+
+
+@pytest.mark.parametrize("D", [16, 32])
+def test_tensor_core_training_gradients_vs_cpu(ns3d, D):
+    """Loss and every parameter block's gradient of the tensor-core training
+    path (forward, input-gradient and weight-gradient convolutions on tcgen05
+    with BF16 operands and FP32 accumulation) against the CPU FP64 reference
+    with the same BF16 weights. Bar for BF16 activations and gradients: loss to
+    1e-2, each block's gradient to 5e-2 relative L2; the FP32 path on the same
+    sample stays at the FP32 bar."""
+    les = ns3d.LES(D, capacity=0, seed=5)
+    assert les.train_path == "tc"
+    les.set_scales(1.2, 0.8)
+    rng = np.random.default_rng(100 + D)
+    u = rng.standard_normal((3, D, D, D)).astype(np.float32)
+    t = rng.standard_normal((6, D, D, D)).astype(np.float32) * 0.1
+    loss, g = les.gradients(u, t)
+    rl, rg, _ = torch_reference(les.weights(), u, t, 1.2, 0.8)
+    assert abs(loss - rl) < 1e-2 * rl, (loss, rl)
+    o = 0
+    for name, n in BLOCKS:
+        a, b = g[o:o + n], rg[o:o + n]
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        print(f"D={D} {name} rel-L2 {err:.2e}")
+        assert err < 5e-2, (name, err)
+        o += n
+    les.set_train_path("fp32")
+    assert les.train_path == "fp32"
+    loss32, g32 = les.gradients(u, t)
+    assert abs(loss32 - rl) < 1e-5 * rl
+    assert np.abs(g32 - rg).max() < 1e-4 * np.abs(rg).max()
+    les.close()
+
+
 @pytest.mark.parametrize("D", [16, 32, 64])
 def test_tensor_core_inference_vs_fp32_network(ns3d, D):
     """The attached-run inference path (tcgen05 implicit-GEMM convolutions,
