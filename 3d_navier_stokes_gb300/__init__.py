@@ -41,6 +41,7 @@ EXPORTS = (
     "ns3d_ensemble_create", "ns3d_ensemble_destroy", "ns3d_ensemble_last_error",
     "ns3d_ensemble_initial_condition", "ns3d_ensemble_set_state_host", "ns3d_ensemble_get_state_host",
     "ns3d_ensemble_measurables", "ns3d_ensemble_get_time", "ns3d_ensemble_step", "ns3d_ensemble_info",
+    "ns3d_ensemble_run",
     "ns3d_ensemble_last_step_ms", "ns3d_set_state_real_host",
     "ns3d_les_num_params", "ns3d_les_create", "ns3d_les_destroy", "ns3d_les_last_error", "ns3d_les_add_snapshot",
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
@@ -211,6 +212,8 @@ def lib():
         L.ns3d_ensemble_get_time.argtypes = [P, I, D, D, ctypes.POINTER(ctypes.c_long)]
         L.ns3d_ensemble_step.restype = I
         L.ns3d_ensemble_step.argtypes = [P, I]
+        L.ns3d_ensemble_run.restype = I
+        L.ns3d_ensemble_run.argtypes = [P, I]
         L.ns3d_ensemble_info.restype = I
         L.ns3d_ensemble_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
         L.ns3d_ensemble_last_step_ms.restype = I
@@ -567,6 +570,10 @@ class Ensemble:
 
     def step(self, nsteps=1):
         self._ck(lib().ns3d_ensemble_step(self._h, nsteps))
+
+    def run(self, nsteps):
+        """nsteps steps in one graph launch (a device-side loop over the captured step)."""
+        self._ck(lib().ns3d_ensemble_run(self._h, nsteps))
 
     def get_state(self, member):
         N = self.members[member]["N"]

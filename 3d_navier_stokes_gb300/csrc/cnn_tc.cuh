@@ -501,28 +501,49 @@ k_wgrad_tc(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict_
         const int x = line >> LOGD, y = line & (D - 1);
         unsigned char* sa = smem + b * WG::STAGE;
         unsigned char* sb = sa + NGRP * WG::A_BYTES;
-        for (int q = tid; q < NGRP * 128 * K8; q += kTcThreads) {
-            const int g = q / (128 * K8), rem = q % (128 * K8), r = rem / K8, k8 = rem % K8;
-            const int t9 = g * TG + r / CI, ci = r % CI;
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (t9 < 9) {
-                const int gx = (x + t9 / 3 - 1) & (D - 1), gy = (y + t9 % 3 - 1) & (D - 1);
-                v = *reinterpret_cast<const uint4*>(a + ci * D3 + (((long long)gx << LOGD) + gy) * D + k8 * 8);
+        // A: four 16-byte chunks per thread and round, all loads before the stores
+        constexpr int NA = NGRP * 128 * K8;
+#pragma unroll 1
+        for (int q0 = tid; q0 < NA; q0 += 4 * kTcThreads) {
+            uint4 v[4];
+            uint32_t off[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = q0 + u * kTcThreads;
+                const int g = q / (128 * K8), rem = q % (128 * K8), r = rem / K8, k8 = rem % K8;
+                const int t9 = g * TG + r / CI, ci = r % CI;
+                v[u] = make_uint4(0u, 0u, 0u, 0u);
+                off[u] = 0xFFFFFFFFu;
+                if (q >= NA) continue;
+                if (t9 < 9) {
+                    const int gx = (x + t9 / 3 - 1) & (D - 1), gy = (y + t9 % 3 - 1) & (D - 1);
+                    v[u] = *reinterpret_cast<const uint4*>(a + ci * D3 + (((long long)gx << LOGD) + gy) * D + k8 * 8);
+                }
+                off[u] = g * WG::A_BYTES + tc_chunk(r, k8, D);
             }
-            *reinterpret_cast<uint4*>(sa + g * WG::A_BYTES + tc_chunk(r, k8, D)) = v;
+#pragma unroll
+            for (int u = 0; u < 4; ++u)
+                if (off[u] != 0xFFFFFFFFu) *reinterpret_cast<uint4*>(sa + off[u]) = v[u];
         }
+        // B: the chunk of z0 .. z0 + 7 of d shifted by dz = j - 1 (periodic), from the
+        // aligned chunk and its neighbour: element pairs re-formed with byte permutes
         for (int q = tid; q < NN * K8; q += kTcThreads) {
             const int n = q / K8, k8 = q % K8, j = n / NB, co = n % NB;
-            const unsigned short* src =
-                reinterpret_cast<const unsigned short*>(d + co * D3 + (((long long)x << LOGD) + y) * D);
-            uint32_t w4[4];
-#pragma unroll
-            for (int e = 0; e < 4; ++e) {
-                const int z0 = k8 * 8 + 2 * e;
-                const uint32_t lo = src[(z0 - (j - 1)) & (D - 1)], hi = src[(z0 + 1 - (j - 1)) & (D - 1)];
-                w4[e] = lo | (hi << 16);
+            const uint4* line = reinterpret_cast<const uint4*>(d + co * D3 + (((long long)x << LOGD) + y) * D);
+            const uint4 c = line[k8];
+            uint4 o;
+            if (j == 1) {
+                o = c;
+            } else if (j == 0) {   // d[z + 1]: elements 1..7 of this chunk, element 0 of the next
+                const uint4 nx = line[(k8 + 1) & (K8 - 1)];
+                o = make_uint4(__byte_perm(c.x, c.y, 0x5432), __byte_perm(c.y, c.z, 0x5432),
+                               __byte_perm(c.z, c.w, 0x5432), __byte_perm(c.w, nx.x, 0x5432));
+            } else {               // d[z - 1]: element 7 of the previous chunk, elements 0..6 of this one
+                const uint4 pv = line[(k8 + K8 - 1) & (K8 - 1)];
+                o = make_uint4(__byte_perm(pv.w, c.x, 0x5432), __byte_perm(c.x, c.y, 0x5432),
+                               __byte_perm(c.y, c.z, 0x5432), __byte_perm(c.z, c.w, 0x5432));
             }
-            *reinterpret_cast<uint4*>(sb + tc_chunk(n, k8, D)) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            *reinterpret_cast<uint4*>(sb + tc_chunk(n, k8, D)) = o;
         }
         fence_proxy_async_smem();
         __syncthreads();

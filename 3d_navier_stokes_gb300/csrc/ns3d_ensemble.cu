@@ -8,6 +8,10 @@
 // viscosity, time step and clock. The groups run on their own streams, and a
 // whole ensemble step is captured once as a CUDA graph in which the groups are
 // parallel branches, so one graph launch advances every member by one step.
+// ns3d_ensemble_run wraps that step in a device-side loop: a graph whose only
+// top-level node is a conditional WHILE node with the step as its body and a
+// one-thread kernel that counts the steps down and clears the condition at
+// zero, so a whole run of n steps is a single graph launch.
 #include <map>
 #include <string.h>
 #include <tuple>
@@ -26,6 +30,8 @@ struct ns3d_ensemble {
     std::vector<std::pair<int, int>> where;   // member -> (group, index in the group)
     cudaStream_t main = nullptr;
     cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t loop = nullptr;            // the step in a device-side while loop
+    long long* d_count = nullptr;              // steps left in the loop
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     char err[512] = {0};
 };
@@ -39,6 +45,8 @@ static void ens_free(ns3d_ensemble* e) {
     if (!e) return;
     if (e->main) cudaStreamSynchronize(e->main);
     if (e->graph) cudaGraphExecDestroy(e->graph);
+    if (e->loop) cudaGraphExecDestroy(e->loop);
+    if (e->d_count) cudaFree(e->d_count);
     for (auto* g : e->groups) delete g;
     for (auto s : e->streams) cudaStreamDestroy(s);
     if (e->main) cudaStreamDestroy(e->main);
@@ -60,6 +68,72 @@ static ns3d_status ens_pass(ns3d_ensemble* e, ns3d::Base* impl, ns3d_status s) {
     return s;
 }
 
+// the loop body's last node: one step done; continue while steps are left
+__global__ void k_loop_count(cudaGraphConditionalHandle h, long long* count) {
+    const long long left = --(*count);
+    cudaGraphSetConditional(h, left > 0 ? 1u : 0u);
+}
+
+// Enqueue one step of every group (forked from and joined back into main).
+static cudaError_t ens_enqueue(ns3d_ensemble* e, cudaEvent_t fork, std::vector<cudaEvent_t>& join) {
+    cudaError_t err = cudaEventRecord(fork, e->main);
+    for (size_t i = 0; err == cudaSuccess && i < e->groups.size(); ++i) {
+        err = cudaStreamWaitEvent(e->streams[i], fork, 0);
+        if (err != cudaSuccess) break;
+        e->groups[i]->enqueue_step();
+        err = cudaEventRecord(join[i], e->streams[i]);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(e->main, join[i], 0);
+    }
+    return err;
+}
+
+static ns3d_status ens_build_loop(ns3d_ensemble* e) {
+    if (e->loop) return NS3D_OK;
+    if (!e->d_count && cudaMalloc(&e->d_count, sizeof(long long)) != cudaSuccess)
+        return ens_fail(e, NS3D_ERR_NOMEM, "loop counter");
+    std::vector<cudaEvent_t> join(e->groups.size());
+    cudaEvent_t fork;
+    if (cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) != cudaSuccess) return NS3D_ERR_CUDA;
+    for (auto& j : join) cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
+    cudaGraph_t g = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    cudaGraphNode_t node = nullptr;
+    cudaError_t err = cudaGraphCreate(&g, 0);
+    // the condition starts at 1 on every launch; the body clears it after the last step
+    if (err == cudaSuccess) err = cudaGraphConditionalHandleCreate(&h, g, 1u, cudaGraphCondAssignDefault);
+    cudaGraphNodeParams np = {};
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    if (err == cudaSuccess) err = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np);
+    if (err == cudaSuccess) {
+        cudaGraph_t body = np.conditional.phGraph_out[0];
+        err = cudaStreamBeginCaptureToGraph(e->main, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+        if (err == cudaSuccess) {
+            cudaError_t e1 = ens_enqueue(e, fork, join);
+            if (e1 == cudaSuccess) {
+                k_loop_count<<<1, 1, 0, e->main>>>(h, e->d_count);
+                e1 = cudaGetLastError();
+            }
+            cudaGraph_t captured = nullptr;
+            err = cudaStreamEndCapture(e->main, &captured);
+            if (err == cudaSuccess) err = e1;
+        }
+    }
+    if (err == cudaSuccess) err = cudaGraphInstantiate(&e->loop, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaEventDestroy(fork);
+    for (auto& j : join) cudaEventDestroy(j);
+    if (err != cudaSuccess) {
+        e->loop = nullptr;
+        cudaGetLastError();
+        snprintf(e->err, sizeof(e->err), "ensemble loop graph: %s", cudaGetErrorString(err));
+        return NS3D_ERR_CUDA;
+    }
+    return NS3D_OK;
+}
+
 static ns3d_status ens_build_graph(ns3d_ensemble* e) {
     if (e->graph) return NS3D_OK;
     std::vector<cudaEvent_t> join(e->groups.size());
@@ -68,14 +142,7 @@ static ns3d_status ens_build_graph(ns3d_ensemble* e) {
     for (auto& j : join) cudaEventCreateWithFlags(&j, cudaEventDisableTiming);
     cudaGraph_t g = nullptr;
     cudaError_t err = cudaStreamBeginCapture(e->main, cudaStreamCaptureModeThreadLocal);
-    if (err == cudaSuccess) err = cudaEventRecord(fork, e->main);
-    for (size_t i = 0; err == cudaSuccess && i < e->groups.size(); ++i) {
-        err = cudaStreamWaitEvent(e->streams[i], fork, 0);
-        if (err != cudaSuccess) break;
-        e->groups[i]->enqueue_step();
-        err = cudaEventRecord(join[i], e->streams[i]);
-        if (err == cudaSuccess) err = cudaStreamWaitEvent(e->main, join[i], 0);
-    }
+    if (err == cudaSuccess) err = ens_enqueue(e, fork, join);
     cudaError_t e2 = cudaStreamEndCapture(e->main, &g);
     if (err == cudaSuccess) err = e2;
     if (err == cudaSuccess) err = cudaGraphInstantiate(&e->graph, g, 0);
@@ -211,6 +278,27 @@ ns3d_status ns3d_ensemble_step(ns3d_ensemble* e, int nsteps) {
     if (cudaEventRecord(e->ev0, e->main) != cudaSuccess) return ens_fail(e, NS3D_ERR_CUDA, "event record");
     for (int k = 0; k < nsteps; ++k)
         if (cudaGraphLaunch(e->graph, e->main) != cudaSuccess) return ens_fail(e, NS3D_ERR_CUDA, "graph launch");
+    if (cudaEventRecord(e->ev1, e->main) != cudaSuccess || cudaStreamSynchronize(e->main) != cudaSuccess)
+        return ens_fail(e, NS3D_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
+    for (auto* g : e->groups) {
+        st = g->status();
+        if (st != NS3D_OK) return ens_pass(e, g, st);
+    }
+    return NS3D_OK;
+}
+
+ns3d_status ns3d_ensemble_run(ns3d_ensemble* e, int nsteps) {
+    if (!e || nsteps < 0) return NS3D_ERR_INVALID;
+    if (nsteps == 0) return NS3D_OK;
+    for (auto s : e->streams)
+        if (cudaStreamSynchronize(s) != cudaSuccess) return ens_fail(e, NS3D_ERR_CUDA, "group stream failed");
+    ns3d_status st = ens_build_loop(e);
+    if (st != NS3D_OK) return st;
+    const long long n = nsteps;
+    if (cudaMemcpyAsync(e->d_count, &n, sizeof(n), cudaMemcpyHostToDevice, e->main) != cudaSuccess)
+        return ens_fail(e, NS3D_ERR_CUDA, "loop counter");
+    if (cudaEventRecord(e->ev0, e->main) != cudaSuccess) return ens_fail(e, NS3D_ERR_CUDA, "event record");
+    if (cudaGraphLaunch(e->loop, e->main) != cudaSuccess) return ens_fail(e, NS3D_ERR_CUDA, "loop graph launch");
     if (cudaEventRecord(e->ev1, e->main) != cudaSuccess || cudaStreamSynchronize(e->main) != cudaSuccess)
         return ens_fail(e, NS3D_ERR_CUDA, cudaGetErrorString(cudaGetLastError()));
     for (auto* g : e->groups) {

@@ -1,6 +1,6 @@
 // tma.cuh — inline-PTX helpers for Blackwell bulk asynchronous copies
-// (cp.async.bulk / cp.async.bulk.tensor) completed through shared-memory
-// mbarriers, with bounded waits.
+// (cp.async.bulk) completed through shared-memory mbarriers, per-thread
+// cp.async copies and L2 prefetches, with bounded waits.
 //
 // Every wait gives up after a budget of SM clock cycles (kWaitCycles, about
 // 2 s at 2 GHz, unless the caller passes a shorter one); the caller then
@@ -65,16 +65,6 @@ __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wai
 // bulk prefetch of global bytes into L2; src 16-byte aligned, bytes % 16 == 0
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-
-// 3D tiled tensor copy global -> shared (coordinates innermost first)
-__device__ __forceinline__ void tensor3_g2s(void* dst, const CUtensorMap* map, int c0, int c1, int c2,
-                                            uint64_t* bar) {
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-        "%4}], [%5];" ::"r"(smem_u32(dst)),
-        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(bar))
-        : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {

@@ -65,7 +65,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--workload", default="forced512",
                     choices=["forced512", "ensemble", "les", "decay256", "closure-infer", "integrators", "fp32err512",
-                             "zgemm"])
+                             "zgemm", "closure-train"])
     ap.add_argument("--err-steps", type=int, default=1000)
     ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
@@ -404,6 +404,8 @@ def run_ensemble(args, local):
     torch.cuda.synchronize()
     clk = Clocks(local)
     ens.step(args.steps)
+    ms_per_launch = ens.last_step_ms()          # one graph launch per step
+    ens.run(args.steps)                         # the same steps in one launch (device-side loop)
     clocks = clk.stop()
     ms = ens.last_step_ms()
     groups, kps = ens.info()
@@ -413,9 +415,11 @@ def run_ensemble(args, local):
             "value": pts * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "batched ensemble, FP32, IF-RK4, CFL 0.5, one graph launch per step",
+            "config": {"workload": "batched ensemble, FP32, IF-RK4, CFL 0.5, the whole run in one graph launch",
                        "members": len(sizes), "launch_groups": groups, "grid_points": pts},
-            "clocks": clocks, "gpu_launches": kps * args.steps,
+            "clocks": clocks, "gpu_launches": (kps + 1) * args.steps,
+            "timing": f"ns3d_ensemble_run: {args.steps} steps in one graph launch (a device-side while loop); "
+                      f"one launch per step: {ms_per_launch / args.steps:.4f} ms/step",
             "autotune": {"seconds": tune_s, "choices": tuned},
             "energy_samples": e0}
     print(json.dumps(line), flush=True)
@@ -508,6 +512,43 @@ def run_closure_infer(args, local):
                       "value": ms, "unit": "ms", "higher_is_better": False, "tflops": flops / (ms * 1e-3) / 1e12,
                       "steps": args.steps, "finite": bool(np.isfinite(tau).all())}), flush=True)
     les.close()
+
+
+def run_closure_train(args, local):
+    """Closure training alone at 64^3: 8 box-filtered snapshots of a seeded forced 256^3 FP32
+    run, then --warmup untimed and --steps timed Adam iterations on each training path (the
+    tensor cores: BF16 operands, FP32 accumulation; and the FP32 CUDA-core kernels), from the
+    same initial weights; ms per iteration (wall clock: each iteration reads its loss back)."""
+    import importlib
+    import torch
+
+    pkg = importlib.import_module("3d_navier_stokes_gb300")
+    torch.cuda.set_device(local)
+    pkg.tuning_load(os.path.join(ROOT, "3d_navier_stokes_gb300", "tuning", "gb300.txt"))
+    dns = pkg.Solver(256, nu=1.5e-3, dt=1e-3, precision="fp32", forcing="SHELL", force_k=2, device=local)
+    dns.InitialConditions("SPECTRUM", seed=0, k0=3.0)
+    dns.RK4Step(20)
+    out = {}
+    for path in ("tc", "fp32"):
+        les = pkg.LES(64, capacity=8, seed=0)
+        les.set_train_path(path)
+        for _ in range(8):
+            dns.RK4Step(2)
+            les.add_snapshot(dns)
+        les.train(max(1, args.warmup), lr=1e-3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        loss = les.train(args.steps, lr=1e-3)
+        t = time.perf_counter() - t0
+        out[path] = {"ms_per_iteration": 1e3 * t / args.steps, "loss_tail": loss}
+        les.close()
+    line = {"metric": "closure training ms per Adam iteration (64^3, 4 conv layers, 32 channels)",
+            "value": out["tc"]["ms_per_iteration"], "unit": "ms", "higher_is_better": False,
+            "steps": args.steps, "warmup": args.warmup, "n_gpus": 1, "data": "synthetic",
+            "dtype": "bf16 operands, f32 accumulation (tc); f32 (fp32)", "paths": out,
+            "speedup_tc_over_fp32": out["fp32"]["ms_per_iteration"] / out["tc"]["ms_per_iteration"],
+            "config": {"workload": "closure training", "Nc": 64, "snapshots": 8, "dns_N": 256}}
+    print(json.dumps(line), flush=True)
 
 
 def run_decay(args, local):
@@ -715,6 +756,9 @@ def main():
         return
     if args.workload == "zgemm":
         run_zgemm(args, local)
+        return
+    if args.workload == "closure-train":
+        run_closure_train(args, local)
         return
     run_ours(args, ws, rank, local)
 

@@ -206,9 +206,14 @@ ns3d_status ns3d_ensemble_measurables(ns3d_ensemble* e, int member, ns3d_measure
 ns3d_status ns3d_ensemble_get_time(ns3d_ensemble* e, int member, double* t, double* dt, long* iters);
 /* every member advances nsteps steps (one graph launch per step) */
 ns3d_status ns3d_ensemble_step(ns3d_ensemble* e, int nsteps);
+/* The same n steps as ONE graph launch: the captured step sits in a
+ * device-side loop (a conditional WHILE graph node whose body ends with a
+ * one-thread kernel that counts the steps down), so the host launches once
+ * per run instead of once per step. Results equal ns3d_ensemble_step's. */
+ns3d_status ns3d_ensemble_run(ns3d_ensemble* e, int nsteps);
 /* number of launch groups and kernels launched per ensemble step */
 ns3d_status ns3d_ensemble_info(ns3d_ensemble* e, int* groups, int* kernels_per_step);
-/* device time of the last ns3d_ensemble_step call, milliseconds */
+/* device time of the last ns3d_ensemble_step / ns3d_ensemble_run call, milliseconds */
 ns3d_status ns3d_ensemble_last_step_ms(ns3d_ensemble* e, float* ms);
 
 /* r2c + 2/3 dealiasing of a host velocity in the reference real layout

@@ -42,3 +42,25 @@ def test_ensemble_matches_single_runs(ns3d, oracle):
     rt, rE, _ = o.measurables()
     assert abs(tot["energy"] - rt[0]) < 1e-12 * rt[0]
     ens.close()
+
+
+def test_ensemble_run_is_one_launch_of_the_same_steps(ns3d):
+    """ns3d_ensemble_run: the captured step in a device-side while loop (one graph
+    launch for the whole run) gives the ensemble's per-step result bit for bit,
+    over two runs in a row (the loop counter is reset by every call)."""
+    members = [dict(N=16, nu=0.02, dt=2e-3, precision="fp64"),
+               dict(N=32, nu=0.004, dt=1e-3, precision="fp32", cfl=0.5),
+               dict(N=48, nu=0.003, dt=1e-3, precision="fp32", forcing="SHELL", force_k=2)]
+    a, b = ns3d.Ensemble(members), ns3d.Ensemble(members)
+    for e in (a, b):
+        for i in range(len(members)):
+            e.InitialConditions(i, "SPECTRUM", seed=30 + i, k0=3.0)
+    a.step(9)
+    a.step(4)
+    b.run(9)
+    b.run(4)
+    for i in range(len(members)):
+        assert np.array_equal(a.get_state(i), b.get_state(i)), i
+        assert a.get_time(i) == b.get_time(i)
+    a.close()
+    b.close()
