@@ -45,6 +45,7 @@ namespace ns3d {
 namespace cnn {
 
 using tc::idesc_bf16;
+using tc::idesc_bf16_mn;
 using tc::mma_bf16;
 using tc::mma_commit;
 using tc::pack_bf16x2;
@@ -80,6 +81,27 @@ template <int LOGD, int KC>
 __device__ __forceinline__ long long blk_index(int x, int y, int z, int kc) {
     constexpr int ZG = (1 << LOGD) / 8;
     return (((((long long)x << LOGD) + y) * ZG + (z >> 3)) * KC + kc) * 8 + (z & 7);
+}
+
+// Operand copies of the weight-gradient kernel, in 16-byte units (8 BF16
+// channels of one point). wg-A [x][y][c/8][z]: the NC channels of one (x, y)
+// line are NC/8 runs of D points. wg-B [x][y][j][c/8][r]: three copies of
+// that, copy j holding the line shifted by dz = j - 1, row r = d[r + 1 - j]
+// (periodic in z), so that one operand of 3 NC rows covers the three dz taps.
+template <int LOGD, int NC>
+__device__ __forceinline__ long long wga_index(int x, int y, int c8, int z) {
+    return ((((long long)x << LOGD) + y) * (NC / 8) + c8) * (1 << LOGD) + z;
+}
+template <int LOGD, int NC>
+__device__ __forceinline__ long long wgb_index(int x, int y, int j, int c8, int r) {
+    return (((((long long)x << LOGD) + y) * 3 + j) * (NC / 8) + c8) * (1 << LOGD) + r;
+}
+// point z's 8 channels c8 into the three copies (rows z - 1, z, z + 1)
+template <int LOGD, int NC>
+__device__ __forceinline__ void wgb_store(uint4* dst, int x, int y, int c8, int z, uint4 v) {
+    constexpr int D = 1 << LOGD;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) dst[wgb_index<LOGD, NC>(x, y, j, c8, (z - 1 + j) & (D - 1))] = v;
 }
 
 // FP32 velocity [3][D^3] x in_scale -> blocked BF16 with 16 channels (KC = 2)
@@ -126,9 +148,10 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cout, int cin
 // D = 1 << LOGD; input BF16 blocked with KC chunks; OUT_MODE 0: GELU(out + b)
 // as BF16 blocked with 4 chunks, 1: (out + b) * out_scale as FP32
 // [cout][D^3]; training: 2: z = out + b to zbuf (FP32 [32][D^3]) and
-// a = GELU(z) both blocked and channel-major (cm, BF16 [32][D^3]);
+// a = GELU(z) blocked and as the wg-A copy (cm) of the weight-gradient kernel;
 // 3 (the input gradient, weights packed transposed and mirrored by
-// k_pack_tc_t, no bias): d = out * GELU'(zbuf) blocked and channel-major. 256 threads: thread 0 issues the copies and the MMAs, every
+// k_pack_tc_t, no bias): d = out * GELU'(zbuf) blocked and as the wg-B copies
+// (cm). 256 threads: thread 0 issues the copies and the MMAs, every
 // warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
 // channels [16 (w / 4), 16 (w / 4) + 16).
 constexpr int kTcThreads = 256;
@@ -298,14 +321,20 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
                     } else {
                         o[j] = v[j] * gelu_grad_tc(zbuf[qi]);
                     }
-                    cm[qi] = __float2bfloat16_rn(o[j]);
                 }
                 uint4* dst = reinterpret_cast<uint4*>(out);
+                uint4* wg = reinterpret_cast<uint4*>(cm);
 #pragma unroll
-                for (int q = 0; q < 2; ++q)
-                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] =
+                for (int q = 0; q < 2; ++q) {
+                    const uint4 pk =
                         make_uint4(pack_bf16x2(o[q * 8 + 0], o[q * 8 + 1]), pack_bf16x2(o[q * 8 + 2], o[q * 8 + 3]),
                                    pack_bf16x2(o[q * 8 + 4], o[q * 8 + 5]), pack_bf16x2(o[q * 8 + 6], o[q * 8 + 7]));
+                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] = pk;
+                    if constexpr (OUT_MODE == 2)
+                        wg[wga_index<LOGD, 32>(x, yy, 2 * half + q, zz)] = pk;
+                    else
+                        wgb_store<LOGD, 32>(wg, x, yy, 2 * half + q, zz, pk);
+                }
             } else {
                 float* dst = reinterpret_cast<float*>(out);
                 const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
@@ -342,8 +371,8 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
 // dW_L[co][ci][t] = sum_p d_L[co][p] a_{L-1}[ci][p + off_t], db_L = sum_p d_L.
 // The forward convolutions (OUT_MODE 2) and the input gradients (OUT_MODE 3,
 // a convolution with the weights transposed and mirrored) run on k_conv3_tc;
-// the weight gradients on k_wgrad_tc, whose operands are "channel-major"
-// BF16 copies [channel][x][y][z] of the activations and gradients that those
+// the weight and bias gradients on k_wgrad_tc, whose operands are the wg-A
+// copies of the activations and the wg-B copies of the gradients that those
 // kernels also write.
 
 // B operand of the input-gradient convolution of a layer with weights
@@ -369,35 +398,35 @@ __global__ void k_pack_tc_t(const __nv_bfloat16* __restrict__ w, int cout, int c
     }
 }
 
-// FP32 velocity [3][D^3] x in_scale -> channel-major BF16 [8][D^3] (channels 3..7 zero)
+// FP32 velocity [3][D^3] x in_scale -> wg-A BF16 with 8 channels (3..7 zero);
+// with one run per line the wg-A index of point p is p
 template <int LOGD>
-__global__ void k_to_cm(const float* __restrict__ u, float in_scale, __nv_bfloat16* __restrict__ dst) {
+__global__ void k_to_wga(const float* __restrict__ u, float in_scale, uint4* __restrict__ dst) {
     constexpr long long D3 = 1ll << (3 * LOGD);
-    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x) {
-#pragma unroll
-        for (int c = 0; c < 8; ++c) dst[c * D3 + p] = __float2bfloat16_rn(c < 3 ? u[c * D3 + p] * in_scale : 0.0f);
-    }
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x)
+        dst[p] = make_uint4(pack_bf16x2(u[p] * in_scale, u[D3 + p] * in_scale), pack_bf16x2(u[2 * D3 + p] * in_scale, 0.0f),
+                            0u, 0u);
 }
 
 // the output gradient d_4 (FP32 [6][D^3]) -> blocked BF16 with 2 chunks (16
-// channels, 6 used) and channel-major BF16 [16][D^3] (channels 6..15 zero)
+// channels, 6 used) and its wg-B copies (channels 6..15 zero)
 template <int LOGD>
-__global__ void k_grad_pack(const float* __restrict__ g, uint4* __restrict__ blk, __nv_bfloat16* __restrict__ cm) {
+__global__ void k_grad_pack(const float* __restrict__ g, uint4* __restrict__ blk, uint4* __restrict__ wg) {
     constexpr int D = 1 << LOGD;
     constexpr long long D3 = (long long)D * D * D;
     for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < D3; p += (long long)gridDim.x * blockDim.x) {
         const int z = (int)(p & (D - 1)), y = (int)((p >> LOGD) & (D - 1)), x = (int)(p >> (2 * LOGD));
         float v[16];
 #pragma unroll
-        for (int c = 0; c < 16; ++c) {
-            v[c] = c < 6 ? g[c * D3 + p] : 0.0f;
-            cm[c * D3 + p] = __float2bfloat16_rn(v[c]);
-        }
+        for (int c = 0; c < 16; ++c) v[c] = c < 6 ? g[c * D3 + p] : 0.0f;
 #pragma unroll
-        for (int q = 0; q < 2; ++q)
-            blk[blk_index<LOGD, 2>(x, y, z, q)] =
+        for (int q = 0; q < 2; ++q) {
+            const uint4 pk =
                 make_uint4(pack_bf16x2(v[q * 8 + 0], v[q * 8 + 1]), pack_bf16x2(v[q * 8 + 2], v[q * 8 + 3]),
                            pack_bf16x2(v[q * 8 + 4], v[q * 8 + 5]), pack_bf16x2(v[q * 8 + 6], v[q * 8 + 7]));
+            blk[blk_index<LOGD, 2>(x, y, z, q)] = pk;
+            wgb_store<LOGD, 16>(wg, x, y, q, z, pk);
+        }
     }
 }
 
@@ -429,45 +458,67 @@ __host__ __device__ constexpr uint32_t tc_chunk(int r, int k8, int K) {
 
 // Weight gradient on the tensor cores. For one z line (x, y) of D points, the
 // GEMM D[(t, ci)][(j, co)] += sum_z a[ci][x + dx_t][y + dy_t][z] d[co][x][y][z - (j - 1)]
-// accumulates dW[co][ci][(t, j)] (t = the (dx, dy) tap, j = dz + 1: the dz taps
-// are the N dimension through z-shifted copies of d). M = 128 rows: TG = 128 / CI
-// (dx, dy) taps of CI channels per tap group, ceil(9 / TG) groups; N = 3 NB;
-// K = the D points of the line, both operands K-major (channel-major sources,
-// 8 consecutive points per 16-byte row). Persistent CTAs walk the D^2 lines,
-// staging line i + 1 (all threads) while the MMAs of line i run (thread 0,
-// double-buffered, bounded waits); each CTA writes its FP32 partial sums
-// [group][128][3 NB] to part, reduced in a fixed order by k_wgrad_reduce.
+// accumulates dW[co][ci][(t, j)] (t = the (dx, dy) tap, j = dz + 1). M = 128
+// rows: TG = 128 / CI taps of CI channels per tap group, NGRP = ceil(9 / TG)
+// groups; N = 3 NB: the three dz copies of the NB output channels; K = the D
+// points of the line. Both operands are MN-major (8 channels of one point per
+// 16-byte row, the K rows of a run 16 bytes apart): A is the nine tap lines of
+// the wg-A copy, one bulk copy each, placed so that the 8-row groups of a tap
+// group are SBO = 16 D bytes apart; B is the wg-B line, one bulk copy. A
+// padding row of the last tap group holds ones, so its j = 1 columns sum to
+// the bias gradient sum_p d[co][p]. Persistent CTAs walk the D^2 lines; thread
+// 0 keeps NST stages of copies in flight and issues the MMAs (bounded waits);
+// each CTA writes its FP32 partial sums [group][128][3 NB] to part, reduced in
+// a fixed order by k_wgrad_reduce.
 template <int CI, int NB, int LOGD>
 struct WgGeo {
-    static constexpr int D = 1 << LOGD, TG = 128 / CI, NGRP = (9 + TG - 1) / TG, NN = 3 * NB, K8 = D / 8;
-    static constexpr uint32_t A_BYTES = 128u * D * 2, B_BYTES = (uint32_t)NN * D * 2;
+    static constexpr int D = 1 << LOGD, TG = 128 / CI, NGRP = (9 + TG - 1) / TG, NN = 3 * NB;
+    static constexpr uint32_t TAP_BYTES = (uint32_t)CI * D * 2;       // one wg-A line
+    static constexpr uint32_t A_BYTES = 128u * D * 2;                 // one tap group
+    static constexpr uint32_t B_BYTES = 3u * NB * D * 2;              // one wg-B line
     static constexpr uint32_t STAGE = NGRP * A_BYTES + B_BYTES;
+    static constexpr int NST = 225280u / STAGE >= 4 ? 4 : (225280u / STAGE >= 3 ? 3 : 2);
+    static constexpr int ONES = (9 - (NGRP - 1) * TG) * CI;          // first padding row of the last group
     static constexpr int TCOLS = tc_pow2(NGRP * NN);
-    static constexpr uint32_t need = 2 * STAGE + 64;
+    static constexpr uint32_t need = NST * STAGE + 2 * NST * 8 + 16;
     // at least enough shared memory that no more CTAs share an SM than its 512 tensor-memory columns hold
     static constexpr uint32_t floor_bytes = 233472u / (512u / (uint32_t)TCOLS + 1u) - 1024u + 16u;
     static constexpr uint32_t SMEM = need > floor_bytes ? need : floor_bytes;
     static constexpr int PART = NGRP * 128 * NN;   // floats of one CTA's partial sums
+    static_assert(CI % 8 == 0 && NB % 16 == 0 && NGRP * TG > 9, "tile shape");
+    static_assert(STAGE % 16 == 0 && TAP_BYTES % 16 == 0 && B_BYTES % 16 == 0, "bulk copy sizes");
+    static_assert(NST * STAGE + 2 * NST * 8 + 16 <= 232448u, "shared memory");
 };
 
 template <int CI, int NB, int LOGD>
 __global__ void __launch_bounds__(kTcThreads, 1)
-k_wgrad_tc(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict__ d, float* __restrict__ part,
+k_wgrad_tc(const uint4* __restrict__ a, const uint4* __restrict__ d, float* __restrict__ part,
            int* __restrict__ status) {
     using WG = WgGeo<CI, NB, LOGD>;
-    constexpr int D = WG::D, TG = WG::TG, NGRP = WG::NGRP, NN = WG::NN, K8 = WG::K8;
-    constexpr long long D3 = (long long)D * D * D;
+    constexpr int D = WG::D, TG = WG::TG, NGRP = WG::NGRP, NN = WG::NN, NST = WG::NST;
     constexpr int nlines = D * D;
-    constexpr uint32_t SBO = K8 * 128;
-    constexpr uint32_t idesc = idesc_bf16(128, NN);
+    constexpr uint32_t SBO = (uint32_t)D * 16;
+    constexpr uint32_t idesc = idesc_bf16_mn(128, NN);
     extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* done = reinterpret_cast<uint64_t*>(smem + 2 * WG::STAGE);
-    uint32_t* holder = reinterpret_cast<uint32_t*>(done + 2);
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem + NST * WG::STAGE);
+    uint64_t* done = full + NST;
+    uint32_t* holder = reinterpret_cast<uint32_t*>(done + NST);
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // zero every stage (the tap slots past the ninth stay zero), then the ones row
+    for (uint32_t q = tid; q < NST * WG::STAGE / 16; q += kTcThreads)
+        reinterpret_cast<uint4*>(smem)[q] = make_uint4(0u, 0u, 0u, 0u);
+    __syncthreads();
+    for (int q = tid; q < NST * D; q += kTcThreads) {
+        unsigned char* row = smem + (q / D) * WG::STAGE + (NGRP - 1) * WG::A_BYTES + (WG::ONES / 8) * SBO + (q % D) * 16;
+        *reinterpret_cast<uint32_t*>(row) = 0x3F80u;   // BF16 1.0 in channel slot 0 of the row group
+    }
+    fence_proxy_async_smem();
     if (tid == 0) {
-        mbar_init(&done[0], 1);
-        mbar_init(&done[1], 1);
+        for (int st = 0; st < NST; ++st) {
+            mbar_init(&full[st], 1);
+            mbar_init(&done[st], 1);
+        }
         fence_barrier_init();
         s_ok = 1;
     }
@@ -479,101 +530,73 @@ k_wgrad_tc(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict_
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *holder;
-    const uint32_t s_u = smem_u32(smem);
-    uint32_t ph[2] = {0u, 0u};
-    bool pend[2] = {false, false};
-    bool ok = true;
-    int it = 0, last = 0;
-    for (int line = blockIdx.x; line < nlines && s_ok; line += gridDim.x, ++it) {
-        const int b = it & 1;
-        if (tid == 0 && pend[b]) {
-            if (ok) ok = mbar_wait(&done[b], ph[b]);
-            if (ok) {
-                ph[b] ^= 1u;
-                pend[b] = false;
-            } else {
-                s_ok = 0;
-                atomicExch(status, kStatusTimeout);
-            }
-        }
-        __syncthreads();
-        if (!s_ok) break;
-        const int x = line >> LOGD, y = line & (D - 1);
-        unsigned char* sa = smem + b * WG::STAGE;
-        unsigned char* sb = sa + NGRP * WG::A_BYTES;
-        // A: four 16-byte chunks per thread and round, all loads before the stores
-        constexpr int NA = NGRP * 128 * K8;
+    if (tid == 0) {
+        const uint32_t s_u = smem_u32(smem);
+        const int first = blockIdx.x, stride = gridDim.x;
+        const int nmine = first < nlines ? (nlines - first + stride - 1) / stride : 0;
+        uint32_t ph_full = 0u, ph_done = 0u, pend_full = 0u, pend_done = 0u;   // one bit per stage
+        auto load = [&](int line, int st) {
+            const int x = line >> LOGD, y = line & (D - 1);
+            unsigned char* sa = smem + st * WG::STAGE;
+            mbar_arrive_expect_tx(&full[st], 9u * WG::TAP_BYTES + WG::B_BYTES);
 #pragma unroll 1
-        for (int q0 = tid; q0 < NA; q0 += 4 * kTcThreads) {
-            uint4 v[4];
-            uint32_t off[4];
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int q = q0 + u * kTcThreads;
-                const int g = q / (128 * K8), rem = q % (128 * K8), r = rem / K8, k8 = rem % K8;
-                const int t9 = g * TG + r / CI, ci = r % CI;
-                v[u] = make_uint4(0u, 0u, 0u, 0u);
-                off[u] = 0xFFFFFFFFu;
-                if (q >= NA) continue;
-                if (t9 < 9) {
-                    const int gx = (x + t9 / 3 - 1) & (D - 1), gy = (y + t9 % 3 - 1) & (D - 1);
-                    v[u] = *reinterpret_cast<const uint4*>(a + ci * D3 + (((long long)gx << LOGD) + gy) * D + k8 * 8);
-                }
-                off[u] = g * WG::A_BYTES + tc_chunk(r, k8, D);
+            for (int t9 = 0; t9 < 9; ++t9) {
+                const int gx = (x + t9 / 3 - 1) & (D - 1), gy = (y + t9 % 3 - 1) & (D - 1);
+                bulk_g2s(sa + (t9 / TG) * WG::A_BYTES + (t9 % TG) * WG::TAP_BYTES,
+                         a + ((((long long)gx << LOGD) + gy) * (CI / 8)) * D, WG::TAP_BYTES, &full[st]);
             }
-#pragma unroll
-            for (int u = 0; u < 4; ++u)
-                if (off[u] != 0xFFFFFFFFu) *reinterpret_cast<uint4*>(sa + off[u]) = v[u];
-        }
-        // B: the chunk of z0 .. z0 + 7 of d shifted by dz = j - 1 (periodic), from the
-        // aligned chunk and its neighbour: element pairs re-formed with byte permutes
-        for (int q = tid; q < NN * K8; q += kTcThreads) {
-            const int n = q / K8, k8 = q % K8, j = n / NB, co = n % NB;
-            const uint4* line = reinterpret_cast<const uint4*>(d + co * D3 + (((long long)x << LOGD) + y) * D);
-            const uint4 c = line[k8];
-            uint4 o;
-            if (j == 1) {
-                o = c;
-            } else if (j == 0) {   // d[z + 1]: elements 1..7 of this chunk, element 0 of the next
-                const uint4 nx = line[(k8 + 1) & (K8 - 1)];
-                o = make_uint4(__byte_perm(c.x, c.y, 0x5432), __byte_perm(c.y, c.z, 0x5432),
-                               __byte_perm(c.z, c.w, 0x5432), __byte_perm(c.w, nx.x, 0x5432));
-            } else {               // d[z - 1]: element 7 of the previous chunk, elements 0..6 of this one
-                const uint4 pv = line[(k8 + K8 - 1) & (K8 - 1)];
-                o = make_uint4(__byte_perm(pv.w, c.x, 0x5432), __byte_perm(c.x, c.y, 0x5432),
-                               __byte_perm(c.y, c.z, 0x5432), __byte_perm(c.z, c.w, 0x5432));
-            }
-            *reinterpret_cast<uint4*>(sb + tc_chunk(n, k8, D)) = o;
-        }
-        fence_proxy_async_smem();
-        __syncthreads();
-        if (tid == 0) {
+            bulk_g2s(sa + NGRP * WG::A_BYTES, d + (((long long)x << LOGD) + y) * 3 * (NB / 8) * D, WG::B_BYTES,
+                     &full[st]);
+            pend_full |= 1u << st;
+        };
+        bool ok = true;
+        for (int st = 0; st < NST && st < nmine; ++st) load(first + st * stride, st);
+#pragma unroll 1
+        for (int i = 0; i < nmine && ok; ++i) {
+            const int st = i % NST;
+            ok = mbar_wait(&full[st], (ph_full >> st) & 1u);
+            if (!ok) break;
+            ph_full ^= 1u << st;
+            pend_full &= ~(1u << st);
             tc_fence_after();
-            const uint32_t a0 = s_u + b * WG::STAGE, b0 = a0 + NGRP * WG::A_BYTES;
+            const uint32_t a0 = s_u + st * WG::STAGE, b0 = a0 + NGRP * WG::A_BYTES;
 #pragma unroll 1
             for (int g = 0; g < NGRP; ++g)
 #pragma unroll 1
                 for (int ks = 0; ks < D / 16; ++ks)
                     mma_bf16(tmem + g * NN, smem_desc(a0 + g * WG::A_BYTES + ks * 256, 128, SBO),
-                             smem_desc(b0 + ks * 256, 128, SBO), idesc, (it > 0 || ks > 0) ? 1u : 0u);
-            mma_commit(&done[b]);
-            pend[b] = true;
-            last = b;
+                             smem_desc(b0 + ks * 256, 128, SBO), idesc, (i > 0 || ks > 0) ? 1u : 0u);
+            mma_commit(&done[st]);
+            pend_done |= 1u << st;
+            // the MMAs of line i - 1 (queued before these) are done: refill their stage
+            if (i >= 1) {
+                const int ps = (i - 1) % NST;
+                ok = mbar_wait(&done[ps], (ph_done >> ps) & 1u);
+                if (!ok) break;
+                ph_done ^= 1u << ps;
+                pend_done &= ~(1u << ps);
+                if (i - 1 + NST < nmine) load(first + (i - 1 + NST) * stride, ps);
+            }
         }
-    }
-    if (tid == 0 && s_ok) {
-        if (ok) ok = mbar_wait(&done[last], ph[last]);
-        if (ok) {
-            ph[last] ^= 1u;
-            pend[last] = false;
-        } else {
+        if (ok && nmine > 0) {
+            const int ls = (nmine - 1) % NST;
+            ok = mbar_wait(&done[ls], (ph_done >> ls) & 1u);
+            if (ok) pend_done &= ~(1u << ls);
+        }
+        if (!ok) {
             s_ok = 0;
             atomicExch(status, kStatusTimeout);
+            // one more bounded wait for the copies and MMAs in flight
+            for (int st = 0; st < NST; ++st) {
+                if (pend_full & (1u << st)) (void)mbar_wait(&full[st], (ph_full >> st) & 1u);
+                if (pend_done & (1u << st)) (void)mbar_wait(&done[st], (ph_done >> st) & 1u);
+            }
         }
     }
+    tc_fence_before();
     __syncthreads();
+    tc_fence_after();
     if (s_ok) {
-        tc_fence_after();
         const int quarter = warp & 3, hh = warp >> 2;
         const int row = quarter * 32 + lane;
         float* dst = part + (long long)blockIdx.x * WG::PART;
@@ -590,29 +613,29 @@ k_wgrad_tc(const __nv_bfloat16* __restrict__ a, const __nv_bfloat16* __restrict_
                                    __uint_as_float(r[4 * j + 3]));
         }
     }
-    if (tid == 0) {
-#pragma unroll
-        for (int b = 0; b < 2; ++b)
-            if (pend[b]) (void)mbar_wait(&done[b], ph[b]);
-    }
     tc_fence_before();
     __syncthreads();
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, WG::TCOLS);
 }
 
-// sum of the CTAs' partials in CTA order, scattered to dW[co][ci][27]
+// sum of the CTAs' partials in CTA order, scattered to dW[co][ci][27]; the
+// ones row's dz = 0 columns to db[co] when db is given
 __global__ void k_wgrad_reduce(const float* __restrict__ part, int nparts, int CI, int NB, int ngrp, int cin,
-                               int cout, float* __restrict__ dw) {
-    const int NN = 3 * NB, TG = 128 / CI, width = ngrp * 128 * NN;
+                               int cout, float* __restrict__ dw, float* __restrict__ db) {
+    const int NN = 3 * NB, TG = 128 / CI, width = ngrp * 128 * NN, ones = (9 - (ngrp - 1) * TG) * CI;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= width) return;
     const int g = e / (128 * NN), r = (e / NN) % 128, n = e % NN;
     const int t9 = g * TG + r / CI, ci = r % CI, j = n / NB, co = n % NB;
-    if (t9 >= 9 || ci >= cin || co >= cout) return;
+    const bool bias = db != nullptr && g == ngrp - 1 && r == ones && j == 1 && co < cout;
+    if (!bias && (t9 >= 9 || ci >= cin || co >= cout)) return;
     float s = 0.0f;
     for (int q = 0; q < nparts; ++q) s += part[(long long)q * width + e];
-    dw[((long long)co * cin + ci) * 27 + t9 * 3 + j] = s;
+    if (bias)
+        db[co] = s;
+    else
+        dw[((long long)co * cin + ci) * 27 + t9 * 3 + j] = s;
 }
 
 }  // namespace cnn

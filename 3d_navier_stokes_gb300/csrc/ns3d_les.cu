@@ -113,9 +113,10 @@ struct ns3d_les : public ns3d::LesHook {
     __nv_bfloat16* wtc = nullptr;                        // packed B operands
     __nv_bfloat16 *act0 = nullptr, *act1 = nullptr, *act2 = nullptr, *act3 = nullptr;   // blocked BF16 activations
     int* dstat = nullptr;                                // device status word
-    // tensor-core training (Nc in {16, 32, 64}): transposed weight packs,
-    // channel-major BF16 activations a0 (8 channels) .. a3 and gradients d1 .. d4
-    // (d4: 16 channels), the weight-gradient partial sums, a zero bias
+    // tensor-core training (Nc in {16, 32, 64}): transposed weight packs, the
+    // weight-gradient operand copies of the activations a0 (wg-A, 8 channels) ..
+    // a3 and of the gradients d1 .. d4 (wg-B, three z-shifted copies; d4: 16 channels), the
+    // weight-gradient partial sums, a zero bias
     __nv_bfloat16* wtc_t = nullptr;
     __nv_bfloat16 *a0cm = nullptr, *a1cm = nullptr, *a2cm = nullptr, *a3cm = nullptr;
     __nv_bfloat16 *d1cm = nullptr, *d2cm = nullptr, *d3cm = nullptr, *d4cm = nullptr;
@@ -175,13 +176,17 @@ struct ns3d_les : public ns3d::LesHook {
     }
 
     // dW of one layer on the tensor cores, reduced into g + off (cin x cout x 27)
+    // (and, with boff >= 0, db of the layer into g + boff)
     template <int CI, int NB, int LOGD>
-    void wgrad_tc(const __nv_bfloat16* a, const __nv_bfloat16* d, int cin, int cout, int off, cudaStream_t s) {
+    void wgrad_tc(const __nv_bfloat16* a, const __nv_bfloat16* d, int cin, int cout, int off, int boff,
+                  cudaStream_t s) {
         using namespace ns3d::cnn;
         using WG = WgGeo<CI, NB, LOGD>;
         const int grid = wg_grid < WG::D * WG::D ? wg_grid : WG::D * WG::D;
-        k_wgrad_tc<CI, NB, LOGD><<<grid, kTcThreads, WG::SMEM, s>>>(a, d, wpart, dstat);
-        k_wgrad_reduce<<<(WG::PART + 255) / 256, 256, 0, s>>>(wpart, grid, CI, NB, WG::NGRP, cin, cout, g + off);
+        k_wgrad_tc<CI, NB, LOGD><<<grid, kTcThreads, WG::SMEM, s>>>(reinterpret_cast<const uint4*>(a),
+                                                                     reinterpret_cast<const uint4*>(d), wpart, dstat);
+        k_wgrad_reduce<<<(WG::PART + 255) / 256, 256, 0, s>>>(wpart, grid, CI, NB, WG::NGRP, cin, cout, g + off,
+                                                             boff >= 0 ? g + boff : nullptr);
     }
 
     // loss and gradients of one sample on the tensor cores (BF16 operands, FP32
@@ -200,7 +205,7 @@ struct ns3d_les : public ns3d::LesHook {
         uint4* b3 = reinterpret_cast<uint4*>(act3);
         const unsigned eg = (unsigned)((D3 + 255) / 256);
         k_to_blocked<LOGD><<<eg, 256, 0, s>>>(u, is, b0);
-        k_to_cm<LOGD><<<eg, 256, 0, s>>>(u, is, a0cm);
+        k_to_wga<LOGD><<<eg, 256, 0, s>>>(u, is, reinterpret_cast<uint4*>(a0cm));
         k_conv3_tc<2, 32, LOGD, 2><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
             b0, W + oT1 / 8, w + ob1, b1, C, 1.f, dstat, z1, a1cm);
         k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
@@ -211,24 +216,21 @@ struct ns3d_les : public ns3d::LesHook {
             b3, W + oT4 / 8, w + ob4, y, 6, 1.f, dstat);
         k_mse<<<NPART, 256, 0, s>>>(y, t, (float)(1.0 / s_out), gy, 6 * D3, part);
         // layer 4: d4 = dloss/dy (blocked into b0, which the forward no longer needs)
-        k_grad_pack<LOGD><<<eg, 256, 0, s>>>(gy, b0, d4cm);
+        k_grad_pack<LOGD><<<eg, 256, 0, s>>>(gy, b0, reinterpret_cast<uint4*>(d4cm));
         k_chan_sum<float><<<6, 256, 0, s>>>(gy, D3, g + ob4);
-        wgrad_tc<32, 16, LOGD>(a3cm, d4cm, C, 6, oW4, s);
+        wgrad_tc<32, 16, LOGD>(a3cm, d4cm, C, 6, oW4, -1, s);
         k_conv3_tc<2, 32, LOGD, 3><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
             b0, WT + oU4 / 8, zeros, b3, C, 1.f, dstat, z3, d3cm);
         // layer 3
-        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d3cm, D3, g + ob3);
-        wgrad_tc<32, 32, LOGD>(a2cm, d3cm, C, C, oW3, s);
+        wgrad_tc<32, 32, LOGD>(a2cm, d3cm, C, C, oW3, ob3, s);
         k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
             b3, WT + oU3 / 8, zeros, b2, C, 1.f, dstat, z2, d2cm);
         // layer 2
-        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d2cm, D3, g + ob2);
-        wgrad_tc<32, 32, LOGD>(a1cm, d2cm, C, C, oW2, s);
+        wgrad_tc<32, 32, LOGD>(a1cm, d2cm, C, C, oW2, ob2, s);
         k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
             b2, WT + oU2 / 8, zeros, b1, C, 1.f, dstat, z1, d1cm);
         // layer 1
-        k_chan_sum<__nv_bfloat16><<<C, 256, 0, s>>>(d1cm, D3, g + ob1);
-        wgrad_tc<8, 32, LOGD>(a0cm, d1cm, 3, C, oW1, s);
+        wgrad_tc<8, 32, LOGD>(a0cm, d1cm, 3, C, oW1, ob1, s);
         cudaMemcpyAsync(part_host, part, sizeof(double) * NPART, cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(part_host + NPART, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
@@ -408,6 +410,7 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
     }
     if (ns3d::cnn::tc_grid_ok(Nc)) {
         const size_t a = sizeof(__nv_bfloat16) * C * (size_t)l->D3;
+        const size_t dpad = 3 * a;   // the three z-shifted wg-B copies of a gradient
         int nsm = 0, dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -417,8 +420,8 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
             cudaMalloc(&l->wtc_t, sizeof(__nv_bfloat16) * kTcTTotal) != cudaSuccess ||
             cudaMalloc(&l->a0cm, a / 4) != cudaSuccess || cudaMalloc(&l->a1cm, a) != cudaSuccess ||
             cudaMalloc(&l->a2cm, a) != cudaSuccess || cudaMalloc(&l->a3cm, a) != cudaSuccess ||
-            cudaMalloc(&l->d1cm, a) != cudaSuccess || cudaMalloc(&l->d2cm, a) != cudaSuccess ||
-            cudaMalloc(&l->d3cm, a) != cudaSuccess || cudaMalloc(&l->d4cm, a / 2) != cudaSuccess ||
+            cudaMalloc(&l->d1cm, dpad) != cudaSuccess || cudaMalloc(&l->d2cm, dpad) != cudaSuccess ||
+            cudaMalloc(&l->d3cm, dpad) != cudaSuccess || cudaMalloc(&l->d4cm, dpad / 2) != cudaSuccess ||
             cudaMalloc(&l->wpart, sizeof(float) * 3 * 128 * 96 * (size_t)(nsm > 0 ? nsm : 1)) != cudaSuccess ||
             cudaMalloc(&l->zeros, sizeof(float) * C) != cudaSuccess || cudaMemset(l->zeros, 0, sizeof(float) * C) != cudaSuccess ||
             les_tc_setup(l) != NS3D_OK) {

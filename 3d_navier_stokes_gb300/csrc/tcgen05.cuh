@@ -10,6 +10,11 @@
 // core matrices) is 128 bytes and its stride byte offset (the next 8 rows) is
 // (K/8) * 128 bytes. One kind::f16 MMA consumes K = 16 (two core matrices,
 // 256 bytes along K).
+//
+// MN-major operands (the weight-gradient kernel): a core matrix is 8 K rows x
+// 16 bytes (8 consecutive M or N elements per row), the leading byte offset is
+// the step between 8-row K groups and the stride byte offset the step between
+// 8-element M/N groups.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -76,6 +81,8 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint
 __host__ __device__ constexpr uint32_t idesc_bf16(int M, int N) {
     return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
+// the same with both operands MN-major (bits 15 and 16, "transpose A / B")
+__host__ __device__ constexpr uint32_t idesc_bf16_mn(int M, int N) { return idesc_bf16(M, N) | (1u << 15) | (1u << 16); }
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
     __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
