@@ -70,6 +70,10 @@ def parse():
     ap.add_argument("--snapshots", type=int, default=2000)
     ap.add_argument("--train-iters", type=int, default=2000)
     ap.add_argument("--les-steps", type=int, default=2000)
+    ap.add_argument("--les-seeds", type=int, default=1,
+                    help="closure networks trained from seeds 0..n-1 on the same data (the spread of the gain)")
+    ap.add_argument("--lr-schedule", default="const", choices=["const", "step"],
+                    help="const: lr 1e-3 throughout; step: 1e-3, 3e-4, 1e-4 over 50 / 30 / 20 %% of the iterations")
     ap.add_argument("--decay-steps", type=int, default=1000)
     return ap.parse_args()
 
@@ -442,54 +446,71 @@ def run_les(args, local):
     dns = pkg.Solver(Nf, nu=nu, dt=dt, precision="fp32", forcing="SHELL", force_k=2, device=local)
     dns.InitialConditions("SPECTRUM", seed=0, k0=3.0)
     dns.RK4Step(500)
-    les = pkg.LES(Nc, capacity=args.snapshots, seed=0)
+    nseed = max(1, args.les_seeds)
+    sched = [(1.0, 1e-3)] if args.lr_schedule == "const" else [(0.5, 1e-3), (0.3, 3e-4), (0.2, 1e-4)]
+    nets = [pkg.LES(Nc, capacity=args.snapshots, seed=s) for s in range(nseed)]
     t0 = time.perf_counter()
     for _ in range(args.snapshots):
         dns.RK4Step(5)
-        les.add_snapshot(dns)
+        for les in nets:
+            les.add_snapshot(dns)
     t_data = time.perf_counter() - t0
-    loss0 = les.dataset_loss()
-    t0 = time.perf_counter()
-    loss_tr = les.train(args.train_iters, lr=1e-3)
-    t_train = time.perf_counter() - t0
-    loss1 = les.dataset_loss()
-    ubar = les.filtered_velocity(dns)
+    loss0 = nets[0].dataset_loss()
+    t_train, loss_tr, loss1 = [], [], []
+    for les in nets:
+        t0 = time.perf_counter()
+        done = 0
+        for i, (frac, lr) in enumerate(sched):
+            it = args.train_iters - done if i == len(sched) - 1 else int(round(frac * args.train_iters))
+            if it > 0:
+                tail = les.train(it, lr=lr)
+            done += it
+        t_train.append(time.perf_counter() - t0)
+        loss_tr.append(tail)
+        loss1.append(les.dataset_loss())
+    ubar = nets[0].filtered_velocity(dns)
     runs = {}
-    for name in ("closure", "plain"):
+    for name in ["plain"] + [f"closure{s}" for s in range(nseed)]:
         c = pkg.Solver(Nc, nu=nu, dt=dt, precision="fp32", forcing="SHELL", force_k=2, device=local)
         c.set_state_real(ubar)
-        if name == "closure":
-            c.attach_closure(les)
+        if name != "plain":
+            c.attach_closure(nets[int(name[7:])])
         runs[name] = c
     ms = {}
     dns.RK4Step(args.les_steps)
     ms["dns"] = dns.last_step_ms() / args.les_steps
-    ms["closure_inference"] = les.profile_infer(20)
+    ms["closure_inference"] = nets[0].profile_infer(20)
     for n, c in runs.items():
         c.RK4Step(args.les_steps)
         ms[n] = c.last_step_ms() / args.les_steps
     ref = pkg.Solver(Nc, nu=nu, dt=dt, precision="fp32", device=local)
-    ref.set_state_real(les.filtered_velocity(dns))
+    ref.set_state_real(nets[0].filtered_velocity(dns))
     _, Eref, _ = ref.ComputeSystemMeasurables()
     k = np.arange(1, Nc // 3 + 1)
     err = {}
     for n, c in runs.items():
         _, E, _ = c.ComputeSystemMeasurables()
         err[n] = float(np.sqrt(np.mean((np.log(E[k]) - np.log(Eref[k])) ** 2)))
-    on, off = runs["closure"].closure_counters()
+    cl = [err[f"closure{s}"] for s in range(nseed)]
+    counters = [runs[f"closure{s}"].closure_counters() for s in range(nseed)]
     line = {"metric": "LES E(k) log-error vs filtered 256^3 DNS (64^3, closure vs plain)",
-            "value": err["closure"], "unit": "rms log E(k) error", "higher_is_better": False,
-            "plain_coarse_error": err["plain"], "n_gpus": 1, "steps": args.les_steps, "dtype": "f32 (bf16 weights)",
+            "value": float(np.mean(cl)), "unit": "rms log E(k) error", "higher_is_better": False,
+            "plain_coarse_error": err["plain"], "closure_error_per_seed": cl,
+            "closure_error_range": [min(cl), max(cl)], "margin_vs_plain": err["plain"] - max(cl),
+            "n_gpus": 1, "steps": args.les_steps, "dtype": "f32 (bf16 weights)",
             "data": "synthetic", "config": {"workload": "learned closure C5", "dns_N": Nf, "les_N": Nc, "nu": nu,
-                                            "dt": dt, "snapshots": args.snapshots, "train_iters": args.train_iters},
-            "ms_per_step": {"dns_256": ms["dns"], "les_64_closure": ms["closure"], "plain_64": ms["plain"],
+                                            "dt": dt, "snapshots": args.snapshots, "train_iters": args.train_iters,
+                                            "seeds": nseed, "lr_schedule": args.lr_schedule},
+            "ms_per_step": {"dns_256": ms["dns"], "les_64_closure": ms["closure0"], "plain_64": ms["plain"],
                             "closure_inference": ms["closure_inference"]},
             "inference_tflops": 126144.0 * Nc ** 3 / (ms["closure_inference"] * 1e-3) / 1e12,
-            "speedup_vs_dns": ms["dns"] / ms["closure"], "closure_steps": on, "fallback_steps": off,
+            "speedup_vs_dns": ms["dns"] / ms["closure0"],
+            "closure_steps": [c[0] for c in counters], "fallback_steps": [c[1] for c in counters],
             "loss": {"before": loss0, "after": loss1, "train_tail": loss_tr},
             "seconds": {"data": t_data, "train": t_train}}
     print(json.dumps(line), flush=True)
-    les.close()
+    for les in nets:
+        les.close()
 
 
 def run_closure_infer(args, local):
