@@ -31,6 +31,9 @@ namespace ns3d {
 
 // e^{-2 pi i m / n} with the quarter-turn reduction used by the transforms.
 void twiddle_table(int n, double* re, double* im);
+// 4D FP32 tensor map without swizzle (ns3d_misc.cu)
+bool encode_map4_f32(CUtensorMap* map, void* base, const uint64_t dims[4], const uint64_t strides[3],
+                     const uint32_t box[4]);
 
 template <typename T, int N, int V = 0>
 class Impl final : public Base {
@@ -160,6 +163,25 @@ class Impl final : public Base {
             NS3D_CK(cudaGetDevice(&dev));
             NS3D_CK(cudaDeviceGetAttribute(&zg_ctas_, cudaDevAttrMultiProcessorCount, dev));
         }
+        if constexpr (xinv_tma_ok<T, N, V>()) {
+            // P1 fed by tensor-tile copies: one map over the 3 M velocity components of U and one of UT
+            const uint64_t dims[4] = {2ull * G::NZP, (uint64_t)N, (uint64_t)N, 3ull * (uint64_t)M_};
+            const uint64_t strides[3] = {sizeof(cx<T>) * (uint64_t)G::NZP, sizeof(cx<T>) * (uint64_t)N * G::NZP,
+                                         sizeof(cx<T>) * (uint64_t)G::FS};
+            const uint32_t box[4] = {2u * (uint32_t)TX, 1u, (uint32_t)xbox_rows<N>(), 1u};
+            if (!encode_map4_f32(&xmap_[0], U_, dims, strides, box) || !encode_map4_f32(&xmap_[1], UT_, dims, strides, box)) {
+                set_err("cuTensorMapEncodeTiled failed for the x-inverse pass");
+                return NS3D_ERR_CUDA;
+            }
+            NS3D_CK(cudaFuncSetAttribute(k_xinv_tma<T, N, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)xinv_tma_smem<T, N, V>()));
+            int per_sm = 0, nsm = 0, dev = 0;
+            NS3D_CK(cudaGetDevice(&dev));
+            NS3D_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+            NS3D_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xinv_tma<T, N, V>, TX * PX::P,
+                                                                  xinv_tma_smem<T, N, V>()));
+            xt_ctas_ = (per_sm > 0 ? per_sm : 1) * nsm;
+        }
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
         NS3D_CK(cudaFuncSetAttribute(k_xfwd<T, N, INT_TAB, X_STAGE1, V>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -191,6 +213,16 @@ class Impl final : public Base {
 
     // each launcher covers members [m0, m0 + cnt); `in` points at member 0's arrays
     void p1(const cx<T>* in, int m0, int cnt) {
+        if constexpr (xinv_tma_ok<T, N, V>()) {
+            const int k = in == U_ ? 0 : (in == UT_ ? 1 : -1);
+            if (k >= 0) {
+                const long long items = (long long)NTX * G::NKY * cnt;
+                const unsigned grid = (unsigned)(items < xt_ctas_ ? items : xt_ctas_);
+                k_xinv_tma<T, N, V><<<grid, TX * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(xmap_[k], 3 * m0, Wm(m0), tw_,
+                                                                                       sdm(m0), cnt);
+                return;
+            }
+        }
         k_xinv<T, N, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_xi(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
     }
     void p2(int m0, int cnt) {
@@ -1040,6 +1072,8 @@ class Impl final : public Base {
     uint4* zg_b_ = nullptr;        // z-pass form 2: DFT matrices (Binv hi, lo, Bfwd hi, lo)
     float* zg_P_ = nullptr;        // z-pass form 2: the three real-space products [member][3][N^3]
     int zg_ctas_ = 0;
+    CUtensorMap xmap_[2];          // P1 tensor-tile form: U and UT as [3 M][N kx][N ky][2 NZP] FP32
+    int xt_ctas_ = 1;
     double* sgs_part_ = nullptr;
     cx<T>* K_ = nullptr;           // RK5 family: stored stages [member][6][3]
     double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]

@@ -374,6 +374,206 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
     store(3, B);
 }
 // ---------------------------------------------------------------------------
+// P1, tensor-tile form (FP32, the x plans of variant 3). Persistent CTAs walk
+// the (member, ky, kz-tile) items inside the circle ky^2 + kz^2 <= KC^2. Thread
+// 0 copies each velocity component of a tile into one of two slabs [kx][TT]
+// with cp.async.bulk.tensor boxes of XB kx rows x TT pencils, only the rows
+// |kx| <= kxmax of the tile's widest column (the rest of a slab is stale and
+// masked like the rows outside the sphere), completion on the slab's mbarrier.
+// Per item: ux and uy are read from their slabs, which then receive this item's
+// uz and the next item's ux; uz is read twice (for wy and for itself) and its
+// slab then receives the next item's uy. Every copy is issued at least two of
+// the item's five transforms before it is read. The transforms and their
+// arithmetic are those of k_xinv (results bit-identical). Waits are bounded;
+// on a timeout the CTA records kStatusTimeout, waits for its own copies and
+// returns.
+// ---------------------------------------------------------------------------
+template <int N> constexpr int xbox_rows() { return N % 32 == 0 ? 32 : 16; }
+template <typename T, int N, int V>
+constexpr size_t xinv_tma_smem() { return sizeof(cx<T>) * (size_t)N * tile_x<T, N, V>() * 3 + 16; }
+template <typename T, int N, int V>
+constexpr bool xinv_tma_ok() {
+    return sizeof(T) == 4 && V == 3 && N % 16 == 0 && N >= 48 && xinv_tma_smem<T, N, V>() <= 232448 &&
+           (2 * tile_x<T, N, V>() * sizeof(T)) % 16 == 0;
+}
+
+template <typename T, int N, int V>
+__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, 1)
+k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw,
+           StepDev* __restrict__ sd, int cnt) {
+    using G = Geo<N>;
+    using PL = typename PlansV<N, V>::X;
+    constexpr int TT = tile_x<T, N, V>();
+    constexpr int E = PL::E, P = PL::P;
+    constexpr int XB = xbox_rows<N>();
+    constexpr uint32_t BOX_BYTES = (uint32_t)XB * TT * sizeof(cx<T>);
+    constexpr int NTX = (G::NZ1 + TT - 1) / TT;
+    constexpr long long PER_MEM = (long long)NTX * G::NKY;
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);       // exchange [N][TT]
+    cx<T>* slab0 = sbuf + (size_t)N * TT;                    // [2][N][TT]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(slab0 + 2 * (size_t)N * TT);
+    const int tid = threadIdx.x;
+    const int t = tid % TT, p = tid / TT;
+    const long long items = PER_MEM * cnt;
+    const T scale = T(1) / (T(N) * T(N) * T(N));
+    const long long budget = sd[0].wait_cycles > 0 ? sd[0].wait_cycles : kWaitCycles;
+    StridedIdx<TT, PL::R1> sidx{t};
+    SyncBlock sync;
+
+    auto next_valid = [&](long long it) {
+        for (; it < items; it += gridDim.x) {
+            const int r = (int)(it % PER_MEM);
+            const int ky = r / NTX - G::KC, kz0 = (r % NTX) * TT;
+            if (ky * ky + kz0 * kz0 <= G::KC2) break;
+        }
+        return it;
+    };
+    // thread 0: component c of item `it` into slab sl
+    auto issue = [&](long long it, int c, int sl) {
+        const int m = (int)(it / PER_MEM), r = (int)(it % PER_MEM);
+        const int ky = r / NTX - G::KC, kz0 = (r % NTX) * TT;
+        const int j = ky < 0 ? ky + N : ky;
+        const int r2 = G::KC2 - ky * ky - kz0 * kz0;
+        int kxm = (int)sqrtf((float)r2);
+        while (kxm * kxm > r2) --kxm;
+        while ((kxm + 1) * (kxm + 1) <= r2) ++kxm;
+        const int nb = kxm / XB + 1;   // boxes covering the rows kx = 0 .. kxm
+        cx<T>* dst = slab0 + (size_t)sl * N * TT;
+        const int cc = c0 + 3 * m + c;
+        fence_proxy_async_smem();
+        if (2 * nb * XB >= N) {
+            mbar_arrive_expect_tx(&bars[sl], (uint32_t)(N / XB) * BOX_BYTES);
+            for (int b = 0; b < N / XB; ++b) tensor4_g2s(dst + (size_t)b * XB * TT, &map, 2 * kz0, j, b * XB, cc, &bars[sl]);
+        } else {
+            mbar_arrive_expect_tx(&bars[sl], (uint32_t)(2 * nb) * BOX_BYTES);
+            for (int b = 0; b < nb; ++b) {
+                const int r_lo = b * XB, r_hi = N - (b + 1) * XB;
+                tensor4_g2s(dst + (size_t)r_lo * TT, &map, 2 * kz0, j, r_lo, cc, &bars[sl]);
+                tensor4_g2s(dst + (size_t)r_hi * TT, &map, 2 * kz0, j, r_hi, cc, &bars[sl]);
+            }
+        }
+    };
+
+    if (tid == 0) {
+        mbar_init(&bars[0], 1);
+        mbar_init(&bars[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    long long it = next_valid(blockIdx.x);
+    int sx = 0, sy = 1;       // slabs holding this item's ux and uy
+    uint32_t ph = 0u;         // bit sl: parity of the next completion of slab sl
+    uint32_t pend = 0u;       // thread 0: slabs with a copy in flight
+    if (tid == 0 && it < items) {
+        issue(it, 0, sx);
+        issue(it, 1, sy);
+        pend = 3u;
+    }
+    // bounded wait of every thread on slab sl; the CTA agrees on the outcome
+    auto wait = [&](int sl) -> bool {
+        const bool ok = __syncthreads_and(mbar_wait(&bars[sl], (ph >> sl) & 1u, budget) ? 1 : 0) != 0;
+        if (ok) {
+            ph ^= 1u << sl;
+            pend &= ~(1u << sl);
+        }
+        return ok;
+    };
+    auto fail = [&](int m) {
+        if (tid == 0) {
+            atomicExch(&sd[m].status, kStatusTimeout);
+            for (int sl = 0; sl < 2; ++sl)
+                if (pend & (1u << sl)) (void)mbar_wait(&bars[sl], (ph >> sl) & 1u, kWaitCycles);
+        }
+    };
+
+    while (it < items) {
+        const int m = (int)(it / PER_MEM), r = (int)(it % PER_MEM);
+        const int ky = r / NTX - G::KC, kz = (r % NTX) * TT + t;
+        const int j = ky < 0 ? ky + N : ky;
+        const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
+        const int rem = G::KC2 - ky * ky - kz * kz;
+        const long long off = (long long)j * G::NZP + kz;
+        const long long xs = (long long)N * G::NZP;
+        cx<T>* Wm = W + (long long)m * 6 * G::FS;
+        const long long nx = next_valid(it + gridDim.x);
+        auto read = [&](int sl, cx<T>(&v)[E]) {
+            const cx<T>* src = slab0 + (size_t)sl * N * TT + t;
+#pragma unroll
+            for (int s = 0; s < E; ++s) {
+                const int kx = kof<N>(p + P * s);
+                v[s] = (colok && kx * kx <= rem) ? src[(size_t)(p + P * s) * TT] * scale : czero<T>();
+            }
+        };
+        auto ikx = [&](cx<T>(&v)[E]) {
+#pragma unroll
+            for (int s = 0; s < E; ++s) v[s] = mul_i(v[s]) * T(kof<N>(p + P * s));
+        };
+        auto store = [&](int f, const cx<T>(&v)[E]) {
+            if (!colok) return;
+            cx<T>* dst = Wm + (long long)f * G::FS + off;
+#pragma unroll
+            for (int s = 0; s < E; ++s) dst[(long long)(p + P * s) * xs] = v[s];
+        };
+        const T fky = T(ky), fkz = T(kz);
+        cx<T> X[E], Y[E], B[E];
+        if (!wait(sx) || !wait(sy)) {
+            fail(m);
+            return;
+        }
+        read(sx, X);
+        read(sy, Y);
+        __syncthreads();   // both slabs read: this item's uz, the next item's ux
+        if (tid == 0) {
+            issue(it, 2, sx);
+            pend |= 1u << sx;
+            if (nx < items) {
+                issue(nx, 0, sy);
+                pend |= 1u << sy;
+            }
+        }
+        // ux; wz = T(i kx uy) - i ky T(ux)
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = Y[s];
+        ikx(B);
+        PL::inv(B, sbuf, p, tw, sidx, sync);
+        PL::inv(X, sbuf, p, tw, sidx, sync);
+        store(0, X);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = B[s] - mul_i(X[s]) * fky;
+        store(5, B);
+        // wy = i kz T(ux) - T(i kx uz)
+        if (!wait(sx)) {
+            fail(m);
+            return;
+        }
+        read(sx, B);
+        ikx(B);
+        PL::inv(B, sbuf, p, tw, sidx, sync);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = mul_i(X[s]) * fkz - B[s];
+        store(4, B);
+        // uz (its slab then takes the next item's uy), uy, wx = i ky T(uz) - i kz T(uy)
+        read(sx, X);
+        __syncthreads();
+        if (tid == 0 && nx < items) {
+            issue(nx, 1, sx);
+            pend |= 1u << sx;
+        }
+        PL::inv(X, sbuf, p, tw, sidx, sync);
+        store(2, X);
+        PL::inv(Y, sbuf, p, tw, sidx, sync);
+        store(1, Y);
+#pragma unroll
+        for (int s = 0; s < E; ++s) B[s] = mul_i(X[s]) * fky - mul_i(Y[s]) * fkz;
+        store(3, B);
+        const int tmp = sx;
+        sx = sy;
+        sy = tmp;
+        it = nx;
+    }
+}
+// ---------------------------------------------------------------------------
 // P2 / P4: FFT along y, in place. grid (ntile, N, nfields).
 // Inverse: inputs only where ky^2 + kz^2 <= KC^2, outputs every y.
 // Forward: inputs every y, outputs only where ky^2 + kz^2 <= KC^2.

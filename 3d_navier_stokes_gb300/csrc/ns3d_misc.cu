@@ -1,6 +1,6 @@
 // ns3d_misc.cu — non-template kernels: the final reduction of the
 // diagnostics and the host-array dealiasing of the C ABI; the host-built DFT
-// matrices of the tensor-core z pass.
+// matrices of the tensor-core z pass; tensor-map encoding.
 #include <string.h>
 
 #include <vector>
@@ -9,6 +9,32 @@
 
 namespace ns3d {
 void twiddle_table(int n, double* re, double* im);
+
+// 4D FP32 tensor map (dims innermost first, byte strides of dims 1..3, box in
+// elements), no swizzle, through the driver's cuTensorMapEncodeTiled; false
+// when the entry point is missing or the encoding is refused
+bool encode_map4_f32(CUtensorMap* map, void* base, const uint64_t dims[4], const uint64_t strides[3],
+                     const uint32_t box[4]) {
+    using encode_fn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+    static encode_fn fn = nullptr;
+    if (!fn) {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess || !f)
+            return false;
+        fn = reinterpret_cast<encode_fn>(f);
+    }
+    const cuuint64_t d[4] = {dims[0], dims[1], dims[2], dims[3]};
+    const cuuint64_t st[3] = {strides[0], strides[1], strides[2]};
+    const cuuint32_t b[4] = {box[0], box[1], box[2], box[3]};
+    const cuuint32_t es[4] = {1, 1, 1, 1};
+    return fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, base, d, st, b, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
 
 // BF16 bits of x, round to nearest even (finite x)
 static uint16_t bf16_bits(float x) {

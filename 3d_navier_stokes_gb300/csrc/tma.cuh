@@ -1,5 +1,6 @@
 // tma.cuh — inline-PTX helpers for Blackwell bulk asynchronous copies
-// (cp.async.bulk) completed through shared-memory mbarriers, per-thread
+// (cp.async.bulk, and tiled tensor copies cp.async.bulk.tensor) completed
+// through shared-memory mbarriers, per-thread
 // cp.async copies and L2 prefetches, with bounded waits.
 //
 // Every wait gives up after a budget of SM clock cycles (kWaitCycles, about
@@ -61,6 +62,18 @@ __device__ __forceinline__ void cp_async(void* dst, const void* src, uint32_t sr
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 // this thread's copies have landed (visible to this thread)
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// tiled tensor copy global -> shared of one box of a 4D tensor map at
+// coordinates (c0 innermost .. c3); c0 x element size must be a multiple of 16
+// bytes. The map lives in kernel parameter space (__grid_constant__).
+__device__ __forceinline__ void tensor4_g2s(void* dst, const CUtensorMap* map, int c0, int c1, int c2, int c3,
+                                            uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
 
 // bulk prefetch of global bytes into L2; src 16-byte aligned, bytes % 16 == 0
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {

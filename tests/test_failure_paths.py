@@ -2,8 +2,9 @@
 defines limits (MIN_STEP_SIZE, MAX_ITERS, MAX_VORT_LIM, data_types.h:130-136)
 but never checks them; this build reports failures as status codes.
 
-* A bounded wait that runs out: the z pass's wait budget is cut to a few
-  clock cycles, so its first wait on an asynchronous copy gives up; the pass
+* A bounded wait that runs out: the wait budget of the copy-fed passes (the
+  z pass, and the tensor-tile x-inverse pass of variant 3) is cut to a few
+  clock cycles, so the first wait on an asynchronous copy gives up; the pass
   lets its copies land, records the timeout and returns, ns3d_step reports
   NS3D_ERR_TIMEOUT, and after the budget is restored the same context steps
   correctly again.
@@ -30,10 +31,12 @@ def dealiased_random(N, seed):
     return uh
 
 
-@pytest.mark.parametrize("N", [64, 256])
-def test_wait_timeout_is_reported_and_recovered(ns3d, oracle, N):
+@pytest.mark.parametrize("N,variant", [(64, None), (256, None), (64, 3)])
+def test_wait_timeout_is_reported_and_recovered(ns3d, oracle, N, variant):
+    """variant 3: the tensor-tile x-inverse pass, the first pass of the step, gives up first."""
     saved = ns3d.tuning(N, "fp32")
-    ns3d.tuning_set(N, saved["variant"] if saved else 0, zform=0, precision="fp32")   # the bulk-copy z pass
+    v = variant if variant is not None else (saved["variant"] if saved else 0)
+    ns3d.tuning_set(N, v, zform=0, precision="fp32")   # the bulk-copy z pass
     try:
         nu, dt = 0.01, 1e-3
         s = ns3d.Solver(N, nu=nu, dt=dt, precision="fp32")
