@@ -147,11 +147,28 @@ __global__ void k_mse(const float* __restrict__ y, const float* __restrict__ t, 
     if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-// Adam (Kingma & Ba 2015) on the FP32 master weights, then their BF16 copy
+// the loss of one sample: the k_mse partial sums in block order, / denom
+__global__ void k_loss_store(const double* __restrict__ part, int nparts, double denom, double* __restrict__ out) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double s = 0.0;
+        for (int i = 0; i < nparts; ++i) s += part[i];
+        *out = s / denom;
+    }
+}
+
+// Adam (Kingma & Ba 2015) on the FP32 master weights, then their BF16 copy.
+// No update once *halt is set, nor when this sample's loss is not finite or a
+// bounded wait of its kernels gave up (*stat != 0): the first such sample sets
+// *halt, so the weights stay those before it.
 __global__ void k_adam(float* __restrict__ w, __nv_bfloat16* __restrict__ wb, const float* __restrict__ g,
                        float* __restrict__ m, float* __restrict__ v, int n, float lr, float b1, float b2, float eps,
-                       float c1, float c2) {
+                       float c1, float c2, const double* __restrict__ loss, const int* __restrict__ stat,
+                       int* __restrict__ halt) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (*halt != 0 || !isfinite(*loss) || *stat != 0) {
+        if (i == 0) *halt = 1;
+        return;
+    }
     if (i >= n) return;
     const float gi = g[i];
     const float mi = b1 * m[i] + (1.0f - b1) * gi;

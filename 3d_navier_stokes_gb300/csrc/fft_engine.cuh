@@ -267,11 +267,12 @@ template <typename T> struct TwOf<cx<T>> {
 // Stage driver.
 //   v      : thread's E elements, v[s] = x[p + P*s] on entry, X[p + P*s] on exit
 //   sbuf   : exchange buffer; sidx(m) maps sequence index m to its slot
-//   tw     : table W_N^m = exp(-2 pi i m / N), m < N (read-only path)
+//   tw     : table W_N^m = exp(-2 pi i m / N), m < N (read-only path); with
+//            TS > 1 the table of a TS times longer transform, read every TS-th entry
 //   sync() : barrier over all threads sharing sbuf
 // Plan::inv computes the inverse as conj(DFT(conj(x))).
 // ---------------------------------------------------------------------------
-template <typename C, bool PK, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
+template <typename C, bool PK, int TS, int N, int E, int Ns, typename SIdx, typename Sync, int R, int... Rest>
 __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                            SIdx sidx, Sync sync) {
     constexpr int P = N / E;
@@ -291,7 +292,7 @@ __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const type
             typename TwOf<C>::type w[R];
             w[0] = TwOf<C>::one();
 #pragma unroll
-            for (int r = 1; r < R; ++r) w[r] = TwOf<C>::at(tw, r * jm * step);
+            for (int r = 1; r < R; ++r) w[r] = TwOf<C>::at(tw, TS * r * jm * step);
             Dft<R, C, PK>::template run_tw<true>(a, w);
         } else {
             Dft<R, C, PK>::run(a);
@@ -310,7 +311,7 @@ __device__ __forceinline__ void fft_stages(C (&v)[E], C* sbuf, int p, const type
 #pragma unroll
         for (int s = 0; s < E; ++s) v[s] = sbuf[sidx(p + s * P)];
         sync();
-        fft_stages<C, PK, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, TS, N, E, Ns * R, SIdx, Sync, Rest...>(v, sbuf, p, tw, sidx, sync);
     }
 }
 
@@ -323,18 +324,19 @@ struct Plan {
     static constexpr int P = N_ / E_;
     static constexpr int nstages = sizeof...(Rs);
     static constexpr int R1 = FirstOf<Rs...>::value;   // radix of the first stage
-    // PK: FP32x2 additions in the butterflies (see vadd)
-    template <bool PK = false, typename C, typename SIdx, typename Sync>
+    // PK: FP32x2 additions in the butterflies (see vadd); TS: twiddle table of a
+    // TS times longer transform
+    template <bool PK = false, int TS = 1, typename C, typename SIdx, typename Sync>
     __device__ __forceinline__ static void fwd(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                                SIdx sidx, Sync sync) {
-        fft_stages<C, PK, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, TS, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
     }
-    template <bool PK = false, typename C, typename SIdx, typename Sync>
+    template <bool PK = false, int TS = 1, typename C, typename SIdx, typename Sync>
     __device__ __forceinline__ static void inv(C (&v)[E_], C* sbuf, int p, const typename TwOf<C>::tab* __restrict__ tw,
                                                SIdx sidx, Sync sync) {
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
-        fft_stages<C, PK, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
+        fft_stages<C, PK, TS, N_, E_, 1, SIdx, Sync, Rs...>(v, sbuf, p, tw, sidx, sync);
 #pragma unroll
         for (int s = 0; s < E_; ++s) v[s] = conjg(v[s]);
     }

@@ -168,7 +168,7 @@ class Impl final : public Base {
             const uint64_t dims[4] = {2ull * G::NZP, (uint64_t)N, (uint64_t)N, 3ull * (uint64_t)M_};
             const uint64_t strides[3] = {sizeof(cx<T>) * (uint64_t)G::NZP, sizeof(cx<T>) * (uint64_t)N * G::NZP,
                                          sizeof(cx<T>) * (uint64_t)G::FS};
-            const uint32_t box[4] = {2u * (uint32_t)TX, 1u, (uint32_t)xbox_rows<N>(), 1u};
+            const uint32_t box[4] = {2u * (uint32_t)xtma_tile<T, N, V>(), 1u, (uint32_t)xbox_rows<N>(), 1u};
             if (!encode_map4_f32(&xmap_[0], U_, dims, strides, box) || !encode_map4_f32(&xmap_[1], UT_, dims, strides, box)) {
                 set_err("cuTensorMapEncodeTiled failed for the x-inverse pass");
                 return NS3D_ERR_CUDA;
@@ -178,8 +178,8 @@ class Impl final : public Base {
             int per_sm = 0, nsm = 0, dev = 0;
             NS3D_CK(cudaGetDevice(&dev));
             NS3D_CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-            NS3D_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xinv_tma<T, N, V>, TX * PX::P,
-                                                                  xinv_tma_smem<T, N, V>()));
+            NS3D_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xinv_tma<T, N, V>,
+                                                                  xtma_tile<T, N, V>() * PX::P, xinv_tma_smem<T, N, V>()));
             xt_ctas_ = (per_sm > 0 ? per_sm : 1) * nsm;
         }
         set_xfwd_attrs<INT_IFRK4>();
@@ -216,9 +216,10 @@ class Impl final : public Base {
         if constexpr (xinv_tma_ok<T, N, V>()) {
             const int k = in == U_ ? 0 : (in == UT_ ? 1 : -1);
             if (k >= 0) {
-                const long long items = (long long)NTX * G::NKY * cnt;
+                constexpr int XT = xtma_tile<T, N, V>();
+                const long long items = (long long)((G::NZ1 + XT - 1) / XT) * G::NKY * cnt;
                 const unsigned grid = (unsigned)(items < xt_ctas_ ? items : xt_ctas_);
-                k_xinv_tma<T, N, V><<<grid, TX * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(xmap_[k], 3 * m0, Wm(m0), tw_,
+                k_xinv_tma<T, N, V><<<grid, XT * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(xmap_[k], 3 * m0, Wm(m0), tw_,
                                                                                        sdm(m0), cnt);
                 return;
             }

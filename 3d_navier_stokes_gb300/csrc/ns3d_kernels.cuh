@@ -389,21 +389,25 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // returns.
 // ---------------------------------------------------------------------------
 template <int N> constexpr int xbox_rows() { return N % 32 == 0 ? 32 : 16; }
+// pencils per CTA and CTAs per SM: variant 3's x tiles, one CTA per SM (8-pencil
+// tiles at two CTAs per SM spill 330 bytes per thread at 512^3 under the 128-register cap)
+template <typename T, int N, int V> constexpr int xtma_tile() { return tile_x<T, N, V>(); }
+template <typename T, int N, int V> constexpr int xtma_minb() { return 1; }
 template <typename T, int N, int V>
-constexpr size_t xinv_tma_smem() { return sizeof(cx<T>) * (size_t)N * tile_x<T, N, V>() * 3 + 16; }
+constexpr size_t xinv_tma_smem() { return sizeof(cx<T>) * (size_t)N * xtma_tile<T, N, V>() * 3 + 16; }
 template <typename T, int N, int V>
 constexpr bool xinv_tma_ok() {
     return sizeof(T) == 4 && V == 3 && N % 16 == 0 && N >= 48 && xinv_tma_smem<T, N, V>() <= 232448 &&
-           (2 * tile_x<T, N, V>() * sizeof(T)) % 16 == 0;
+           (2 * xtma_tile<T, N, V>() * sizeof(T)) % 16 == 0;
 }
 
 template <typename T, int N, int V>
-__global__ void __launch_bounds__(tile_x<T, N, V>() * PlansV<N, V>::X::P, 1)
+__global__ void __launch_bounds__(xtma_tile<T, N, V>() * PlansV<N, V>::X::P, xtma_minb<T, N, V>())
 k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw,
            StepDev* __restrict__ sd, int cnt) {
     using G = Geo<N>;
     using PL = typename PlansV<N, V>::X;
-    constexpr int TT = tile_x<T, N, V>();
+    constexpr int TT = xtma_tile<T, N, V>();
     constexpr int E = PL::E, P = PL::P;
     constexpr int XB = xbox_rows<N>();
     constexpr uint32_t BOX_BYTES = (uint32_t)XB * TT * sizeof(cx<T>);
@@ -813,6 +817,16 @@ constexpr int ZLINE_WARPS = 4;
 template <int N> struct ZPlan { using A = typename Plans<N>::A; };
 template <int N> constexpr int zline_gw() { return ZPlan<N>::A::P > 32 ? ZPlan<N>::A::P / 32 : 1; }
 template <int N> constexpr int zline_gpw() { return ZPlan<N>::A::P <= 32 ? 32 / ZPlan<N>::A::P : 1; }
+// the real Nz line as a half-length complex transform where a plan of N/2 points
+// runs on the same lanes with half the elements
+template <int N> constexpr bool zline_half_nz() {
+    if constexpr (N % 2 != 0 || N < 256 || (N & (N - 1)) != 0) {
+        return false;
+    } else {
+        using HP = typename Plans<N / 2>::X;
+        return HP::P == ZPlan<N>::A::P && 2 * HP::E == ZPlan<N>::A::E;
+    }
+}
 template <typename T, int N>
 constexpr bool zline_ok() {
     constexpr int P = ZPlan<N>::A::P;
@@ -1001,13 +1015,45 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
             }
         }
         sync();
-        // Nz (real input): its spectrum is the transform itself
-        PL::template fwd<kPK>(V2, sb, p, tw, sidx, sync);
         cx<T>* outC = Wm + 2 * G::FS + line * NZP;
+        if constexpr (zline_half_nz<N>()) {
+            // Nz (real input) by a half-length transform: z[n] = Nz[2n] + i Nz[2n + 1]
+            // (the real line through the exchange buffer), Z = DFT_{N/2}(z) with every
+            // second twiddle of the N table, then for k <= KC
+            //   X[k] = (Z[k] + conj Z[N/2 - k]) / 2 - i W_N^k (Z[k] - conj Z[N/2 - k]) / 2
+            using HP = typename Plans<N / 2>::X;
+            constexpr int EH = HP::E, M2 = N / 2;
+            T* sr = reinterpret_cast<T*>(sb);
 #pragma unroll
-        for (int q = 0; q < E; ++q) {
-            const int m = p + P * q;
-            if (P * q <= G::KC && m <= G::KC) outC[m] = V2[q];
+            for (int q = 0; q < E; ++q) sr[p + P * q] = V2[q].x;
+            sync();
+            cx<T> Z[EH];
+#pragma unroll
+            for (int q = 0; q < EH; ++q) Z[q] = reinterpret_cast<const cx<T>*>(sr)[p + P * q];
+            sync();
+            HP::template fwd<kPK, 2>(Z, sb, p, tw, sidx, sync);
+#pragma unroll
+            for (int q = 0; q < EH; ++q) sb[sidx(p + P * q)] = Z[q];
+            sync();
+            const T half = T(0.5);
+#pragma unroll
+            for (int q = 0; q < EH; ++q) {
+                const int k = p + P * q;
+                if (P * q <= G::KC && k <= G::KC) {
+                    const cx<T> zc = conjg(sb[sidx((M2 - k) % M2)]);
+                    const cx<T> e = (Z[q] + zc) * half, d = (Z[q] - zc) * half;
+                    const cx<T> wd = cmul(ldg(&tw[k]), d);
+                    outC[k] = mk(e.x + wd.y, e.y - wd.x);
+                }
+            }
+        } else {
+            // Nz (real input): its spectrum is the transform itself
+            PL::template fwd<kPK>(V2, sb, p, tw, sidx, sync);
+#pragma unroll
+            for (int q = 0; q < E; ++q) {
+                const int m = p + P * q;
+                if (P * q <= G::KC && m <= G::KC) outC[m] = V2[q];
+            }
         }
         // the stage buffer is refilled by a bulk copy (async proxy) next iteration:
         // order every lane's exchange accesses to it before that

@@ -82,6 +82,7 @@ constexpr int C = 32;   // hidden channels
 constexpr int oW1 = 0, ob1 = oW1 + C * 3 * 27, oW2 = ob1 + C, ob2 = oW2 + C * C * 27, oW3 = ob2 + C,
               ob3 = oW3 + C * C * 27, oW4 = ob3 + C, ob4 = oW4 + 6 * C * 27, NPARAM = ob4 + 6;
 constexpr int NPART = 256;
+constexpr int kTrainChunk = 64;   // Adam iterations queued between host checks of the losses
 // packed tensor-core B operands of the four layers (BF16 elements):
 // (KC, NO) = (2, 32), (4, 32), (4, 32), (4, 16); 9 x 3 NO x 8 KC each
 constexpr int kTcW1 = 9 * 96 * 2 * 8, kTcW2 = 9 * 96 * 4 * 8, kTcW4 = 9 * 48 * 4 * 8;
@@ -122,6 +123,11 @@ struct ns3d_les : public ns3d::LesHook {
     __nv_bfloat16 *d1cm = nullptr, *d2cm = nullptr, *d3cm = nullptr, *d4cm = nullptr;
     float* wpart = nullptr;
     float* zeros = nullptr;
+    // training: the losses of one chunk of Adam iterations (device, pinned host) and
+    // the device word that stops the updates after a non-finite loss or a failed wait
+    double* losses = nullptr;
+    double* losses_host = nullptr;
+    int* halt = nullptr;
     int wg_grid = 0;
     int train_path = 0;                                  // 0: tensor cores where compiled, 1: FP32 CUDA cores
     int tc_grid[3] = {0, 0, 0};                          // CTAs of the three kernel shapes
@@ -143,8 +149,8 @@ struct ns3d_les : public ns3d::LesHook {
                                                                   out_scale);
     }
 
-    // loss and gradients of one sample (u raw velocity, t raw stress); returns the loss
-    double fwd_bwd(const float* u, const float* t, cudaStream_t s) {
+    // loss partial sums (part) and gradients (g) of one sample (u raw velocity, t raw stress)
+    void fwd_bwd(const float* u, const float* t, cudaStream_t s) {
         using namespace ns3d::cnn;
         const float is = (float)(1.0 / s_in);
         fwd(u, y, is, 1.f, s);
@@ -156,11 +162,6 @@ struct ns3d_les : public ns3d::LesHook {
         k_conv3_wgrad<true><<<C * C, 256, 0, s>>>(gz2, z1, g + oW2, g + ob2, C, Nc, 1.f);
         k_conv3<C, C, false, true, true><<<grid(), 256, 0, s>>>(gz2, wb + oW2, nullptr, z1, gz1, Nc, 1.f, 1.f);
         k_conv3_wgrad<false><<<C * 3, 256, 0, s>>>(gz1, u, g + oW1, g + ob1, 3, Nc, is);
-        cudaMemcpyAsync(part_host, part, sizeof(double) * NPART, cudaMemcpyDeviceToHost, s);
-        cudaStreamSynchronize(s);
-        double l = 0.0;
-        for (int i = 0; i < NPART; ++i) l += part_host[i];
-        return l / (double)(6 * D3);
     }
 
     bool tc() const { return ns3d::cnn::tc_grid_ok(Nc) && wtc != nullptr; }
@@ -193,7 +194,7 @@ struct ns3d_les : public ns3d::LesHook {
     // accumulation): forward with the pre-activations kept, then per layer the
     // bias and weight gradients and the input gradient
     template <int LOGD>
-    double fwd_bwd_tc_d(const float* u, const float* t, cudaStream_t s) {
+    void fwd_bwd_tc_d(const float* u, const float* t, cudaStream_t s) {
         using namespace ns3d::cnn;
         constexpr int D = 1 << LOGD;
         const float is = (float)(1.0 / s_in);
@@ -231,22 +232,27 @@ struct ns3d_les : public ns3d::LesHook {
             b2, WT + oU2 / 8, zeros, b1, C, 1.f, dstat, z1, d1cm);
         // layer 1
         wgrad_tc<8, 32, LOGD>(a0cm, d1cm, 3, C, oW1, ob1, s);
-        cudaMemcpyAsync(part_host, part, sizeof(double) * NPART, cudaMemcpyDeviceToHost, s);
+    }
+    void fwd_bwd_tc(const float* u, const float* t, cudaStream_t s) {
+        if (Nc == 16) fwd_bwd_tc_d<4>(u, t, s);
+        else if (Nc == 32) fwd_bwd_tc_d<5>(u, t, s);
+        else fwd_bwd_tc_d<6>(u, t, s);
+    }
+    // the training path's gradients (tensor cores where compiled and selected), and
+    // the sample's loss into the device slot *loss_slot
+    void fwd_bwd_train(const float* u, const float* t, double* loss_slot, cudaStream_t s) {
+        if (tc_train()) fwd_bwd_tc(u, t, s);
+        else fwd_bwd(u, t, s);
+        ns3d::cnn::k_loss_store<<<1, 32, 0, s>>>(part, NPART, (double)(6 * D3), loss_slot);
+    }
+    // the same, synchronously: the loss, or NaN when a bounded wait gave up
+    double fwd_bwd_sync(const float* u, const float* t, cudaStream_t s) {
+        fwd_bwd_train(u, t, losses, s);
+        cudaMemcpyAsync(losses_host, losses, sizeof(double), cudaMemcpyDeviceToHost, s);
         cudaMemcpyAsync(part_host + NPART, dstat, sizeof(int), cudaMemcpyDeviceToHost, s);
         cudaStreamSynchronize(s);
-        if (*reinterpret_cast<const int*>(part_host + NPART) != 0) return NAN;   // a bounded wait gave up
-        double l = 0.0;
-        for (int i = 0; i < NPART; ++i) l += part_host[i];
-        return l / (double)(6 * D3);
-    }
-    double fwd_bwd_tc(const float* u, const float* t, cudaStream_t s) {
-        if (Nc == 16) return fwd_bwd_tc_d<4>(u, t, s);
-        if (Nc == 32) return fwd_bwd_tc_d<5>(u, t, s);
-        return fwd_bwd_tc_d<6>(u, t, s);
-    }
-    // the training path's loss and gradients (tensor cores where compiled and selected)
-    double fwd_bwd_train(const float* u, const float* t, cudaStream_t s) {
-        return tc_train() ? fwd_bwd_tc(u, t, s) : fwd_bwd(u, t, s);
+        if (*reinterpret_cast<const int*>(part_host + NPART) != 0) return NAN;
+        return losses_host[0];
     }
 
     // B operands of the tensor-core layers from the current BF16 weights
@@ -297,9 +303,10 @@ struct ns3d_les : public ns3d::LesHook {
                         (void*)z2, (void*)z3, (void*)y, (void*)gy, (void*)gz3, (void*)gz2, (void*)gz1, (void*)io_u,
                         (void*)io_t, (void*)part, (void*)wtc, (void*)act0, (void*)act1, (void*)act2, (void*)act3,
                         (void*)dstat, (void*)wtc_t, (void*)a0cm, (void*)a1cm, (void*)a2cm, (void*)a3cm, (void*)d1cm,
-                        (void*)d2cm, (void*)d3cm, (void*)d4cm, (void*)wpart, (void*)zeros})
+                        (void*)d2cm, (void*)d3cm, (void*)d4cm, (void*)wpart, (void*)zeros, (void*)losses, (void*)halt})
             if (q) cudaFree(q);
         if (part_host) cudaFreeHost(part_host);
+        if (losses_host) cudaFreeHost(losses_host);
         if (stream) cudaStreamDestroy(stream);
     }
 };
@@ -382,6 +389,9 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
         cudaMalloc(&l->io_u, f * 3 * l->D3) != cudaSuccess || cudaMalloc(&l->io_t, f * 6 * l->D3) != cudaSuccess ||
         cudaMalloc(&l->part, sizeof(double) * NPART) != cudaSuccess ||
         cudaMallocHost(&l->part_host, sizeof(double) * (NPART + 1)) != cudaSuccess ||
+        cudaMalloc(&l->losses, sizeof(double) * kTrainChunk) != cudaSuccess ||
+        cudaMallocHost(&l->losses_host, sizeof(double) * kTrainChunk) != cudaSuccess ||
+        cudaMalloc(&l->halt, sizeof(int)) != cudaSuccess ||
         (capacity > 0 && (cudaMalloc(&l->data_u, f * 3 * l->D3 * capacity) != cudaSuccess ||
                           cudaMalloc(&l->data_t, f * 6 * l->D3 * capacity) != cudaSuccess))) {
         delete l;
@@ -525,30 +535,46 @@ ns3d_status ns3d_les_train(ns3d_les* l, int iterations, double lr, double* mean_
     if (!l || iterations < 0 || !(lr > 0)) return NS3D_ERR_INVALID;
     ns3d_status st = les_auto_scales(l);
     if (st != NS3D_OK) return st;
+    LES_CK(cudaMemsetAsync(l->halt, 0, sizeof(int), l->stream));
     double acc = 0.0;
     int nacc = 0;
-    for (int it = 0; it < iterations; ++it) {
-        const int smp = (int)(sm64(l->rng) % (unsigned long long)l->count);
-        const double loss = l->fwd_bwd_train(l->data_u + 3 * l->D3 * smp, l->data_t + 6 * l->D3 * smp, l->stream);
-        if (!isfinite(loss)) {
-            int st = 0;
-            cudaMemcpy(&st, l->dstat, sizeof(int), cudaMemcpyDeviceToHost);
-            if (st != 0) return les_fail(l, NS3D_ERR_TIMEOUT, "a bounded wait in a tensor-core training kernel gave up");
-            return les_fail(l, NS3D_ERR_NUMERIC, "training loss is not finite");
+    const float b1 = 0.9f, b2 = 0.999f;
+    // chunks of kTrainChunk iterations queued without host round trips; the samples come
+    // from the host generator, each loss goes to its device slot, and the host reads the
+    // chunk's losses and status once it is done
+    for (int it0 = 0; it0 < iterations; it0 += kTrainChunk) {
+        const int n = iterations - it0 < kTrainChunk ? iterations - it0 : kTrainChunk;
+        for (int k = 0; k < n; ++k) {
+            const int smp = (int)(sm64(l->rng) % (unsigned long long)l->count);
+            l->fwd_bwd_train(l->data_u + 3 * l->D3 * smp, l->data_t + 6 * l->D3 * smp, l->losses + k, l->stream);
+            const long long t = l->adam_t + 1 + k;
+            const float c1 = 1.0f - powf(b1, (float)t), c2 = 1.0f - powf(b2, (float)t);
+            ns3d::cnn::k_adam<<<(NPARAM + 255) / 256, 256, 0, l->stream>>>(
+                l->w, l->wb, l->g, l->m, l->v, NPARAM, (float)lr, b1, b2, 1e-8f, c1, c2, l->losses + k, l->dstat, l->halt);
+            if (l->tc_train()) {   // the next sample's tensor-core layers read the updated weights
+                l->pack_tc(l->stream);
+                l->pack_tc_t(l->stream);
+            }
         }
-        l->adam_t++;
-        const float b1 = 0.9f, b2 = 0.999f;
-        const float c1 = 1.0f - powf(b1, (float)l->adam_t), c2 = 1.0f - powf(b2, (float)l->adam_t);
-        ns3d::cnn::k_adam<<<(NPARAM + 255) / 256, 256, 0, l->stream>>>(l->w, l->wb, l->g, l->m, l->v, NPARAM,
-                                                                      (float)lr, b1, b2, 1e-8f, c1, c2);
-        if (l->tc_train()) {   // the next sample's tensor-core layers read the updated weights
-            l->pack_tc(l->stream);
-            l->pack_tc_t(l->stream);
+        LES_CK(cudaMemcpyAsync(l->losses_host, l->losses, sizeof(double) * n, cudaMemcpyDeviceToHost, l->stream));
+        LES_CK(cudaMemcpyAsync(l->part_host + NPART, l->dstat, sizeof(int), cudaMemcpyDeviceToHost, l->stream));
+        LES_CK(cudaStreamSynchronize(l->stream));
+        for (int k = 0; k < n; ++k) {
+            if (!isfinite(l->losses_host[k]) || *reinterpret_cast<const int*>(l->part_host + NPART) != 0) {
+                l->adam_t += k;   // the updates before the first bad sample were applied
+                l->pack_tc(l->stream);
+                cudaStreamSynchronize(l->stream);
+                if (*reinterpret_cast<const int*>(l->part_host + NPART) != 0)
+                    return les_fail(l, NS3D_ERR_TIMEOUT, "a bounded wait in a tensor-core training kernel gave up");
+                return les_fail(l, NS3D_ERR_NUMERIC, "training loss is not finite");
+            }
+            const int it = it0 + k;
+            if (it >= iterations - iterations / 10 - 1) {
+                acc += l->losses_host[k];
+                nacc++;
+            }
         }
-        if (it >= iterations - iterations / 10 - 1) {
-            acc += loss;
-            nacc++;
-        }
+        l->adam_t += n;
     }
     l->pack_tc(l->stream);
     LES_CK(cudaStreamSynchronize(l->stream));
@@ -592,7 +618,7 @@ ns3d_status ns3d_les_gradients_host(ns3d_les* l, const float* u, const float* ta
     if (!l || !u || !tau) return NS3D_ERR_INVALID;
     LES_CK(cudaMemcpy(l->io_u, u, sizeof(float) * 3 * l->D3, cudaMemcpyHostToDevice));
     LES_CK(cudaMemcpy(l->io_t, tau, sizeof(float) * 6 * l->D3, cudaMemcpyHostToDevice));
-    const double ls = l->fwd_bwd_train(l->io_u, l->io_t, l->stream);
+    const double ls = l->fwd_bwd_sync(l->io_u, l->io_t, l->stream);
     if (loss) *loss = ls;
     if (grads) LES_CK(cudaMemcpy(grads, l->g, sizeof(float) * NPARAM, cudaMemcpyDeviceToHost));
     return NS3D_OK;

@@ -61,6 +61,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--shape", type=int, nargs=2, metavar=("VARIANT", "ZFORM"),
+                    help="run this tile variant and z-pass form (no autotuning)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--workload", default="forced512",
@@ -250,7 +252,10 @@ def run_ours(args, ws, rank, local):
     N = args.N
     cfg = dict(nu=nu_for(N), dt=1e-3, cfl=0.5, precision="fp32", forcing="SHELL", force_k=2, device=local)
     tuned = None
-    if not args.no_autotune:
+    if args.shape:
+        pkg.tuning_set(N, args.shape[0], zform=args.shape[1], precision="fp32")
+        tuned = {"N": N, "variant": args.shape[0], "zform": args.shape[1], "chosen_by": "--shape"}
+    elif not args.no_autotune:
         # the library's autotuner picks the tile / radix variant and z-pass form of this size (untimed)
         tuned, tried = pkg.autotune(N, steps=20, **cfg)
         tuned = dict(tuned, tried=[[t["variant"], t["zform"], round(t["ms_per_step"], 4)] for t in tried])
