@@ -182,6 +182,117 @@ void orc_fft_plan_destroy(orc_fft_plan_t* q) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* Batched Stockham FFT (radix 4, 2, 3) of B interleaved lines, x[j * B + b]: */
+/* the 3D transforms below gather blocks of B contiguous columns, so every   */
+/* memory access is a contiguous run, and each stage reads its twiddles from */
+/* a per-stage table. Stage with Ns = product of the earlier radices and      */
+/* radix R: element j (j < n / R) reads x[j + r n / R], multiplies by          */
+/* W_n^{r (j mod Ns) n / (Ns R)}, takes the R-point DFT and writes output r to */
+/* (j / Ns) Ns R + (j mod Ns) + r Ns (the self-sorting Stockham order of       */
+/* Govindaraju et al., SC 2008). Complex products are written out in real     */
+/* arithmetic. Lengths with another prime factor use the per-line transform. */
+/* ------------------------------------------------------------------------ */
+#define ORC_BCOLS 16   /* columns per block of the x and y passes */
+
+typedef struct {
+    int n, nst, ok;
+    int rad[40];
+    cplx* tw[40];      /* stage s: tw[r * Ns + jm], r < R, jm < Ns */
+} bplan;
+
+static inline cplx mul_i(cplx a) { return CMPLX(-cimag(a), creal(a)); }   /* i a */
+static inline cplx cm(cplx a, cplx b) {
+    const double ar = creal(a), ai = cimag(a), br = creal(b), bi = cimag(b);
+    return CMPLX(ar * br - ai * bi, ar * bi + ai * br);
+}
+
+static void bplan_init(bplan* p, int n) {
+    memset(p, 0, sizeof *p);
+    p->n = n;
+    int m = n;
+    while (m % 4 == 0) { p->rad[p->nst++] = 4; m /= 4; }
+    while (m % 2 == 0) { p->rad[p->nst++] = 2; m /= 2; }
+    while (m % 3 == 0) { p->rad[p->nst++] = 3; m /= 3; }
+    p->ok = (m == 1);
+    if (!p->ok) { p->nst = 0; return; }
+    int Ns = 1;
+    for (int s = 0; s < p->nst; ++s) {
+        const int R = p->rad[s];
+        p->tw[s] = (cplx*)malloc(sizeof(cplx) * (size_t)R * Ns);
+        for (int r = 0; r < R; ++r)
+            for (int jm = 0; jm < Ns; ++jm) p->tw[s][r * Ns + jm] = twiddle((long)r * jm * (n / (Ns * R)), n);
+        Ns *= R;
+    }
+}
+
+static void bplan_free(bplan* p) {
+    for (int s = 0; s < p->nst; ++s) free(p->tw[s]);
+    p->nst = 0;
+}
+
+/* forward transform of the B lines of x (y: scratch of the same size) */
+static void bfft(const bplan* p, cplx* x, cplx* y, int B) {
+    const int n = p->n;
+    cplx* src = x;
+    cplx* dst = y;
+    int Ns = 1;
+    for (int s = 0; s < p->nst; ++s) {
+        const int R = p->rad[s], Q = n / R;
+        const cplx* tw = p->tw[s];
+        const size_t is = (size_t)Q * B, os = (size_t)Ns * B;
+        for (int j = 0; j < Q; ++j) {
+            const int jm = j % Ns;
+            const cplx* in = src + (size_t)j * B;
+            cplx* out = dst + ((size_t)(j / Ns) * Ns * R + jm) * B;
+            if (R == 4) {
+                const cplx w1 = tw[Ns + jm], w2 = tw[2 * Ns + jm], w3 = tw[3 * Ns + jm];
+                for (int b = 0; b < B; ++b) {
+                    const cplx a0 = in[b], a1 = cm(in[is + b], w1), a2 = cm(in[2 * is + b], w2),
+                               a3 = cm(in[3 * is + b], w3);
+                    const cplx s02 = a0 + a2, d02 = a0 - a2, s13 = a1 + a3, t = a1 - a3;
+                    const cplx d13 = CMPLX(cimag(t), -creal(t));   /* -i (a1 - a3) */
+                    out[b] = s02 + s13;
+                    out[os + b] = d02 + d13;
+                    out[2 * os + b] = s02 - s13;
+                    out[3 * os + b] = d02 - d13;
+                }
+            } else if (R == 2) {
+                const cplx w1 = tw[Ns + jm];
+                for (int b = 0; b < B; ++b) {
+                    const cplx a0 = in[b], a1 = cm(in[is + b], w1);
+                    out[b] = a0 + a1;
+                    out[os + b] = a0 - a1;
+                }
+            } else {   /* R == 3: X1,2 = a0 - (a1 + a2) / 2 -+ i (sqrt(3) / 2) (a1 - a2) */
+                const cplx w1 = tw[Ns + jm], w2 = tw[2 * Ns + jm];
+                const double h = 0.86602540378443864676;
+                for (int b = 0; b < B; ++b) {
+                    const cplx a0 = in[b], a1 = cm(in[is + b], w1), a2 = cm(in[2 * is + b], w2);
+                    const cplx t1 = a1 + a2, t2 = a0 - 0.5 * t1, d = a1 - a2;
+                    const cplx t3 = CMPLX(h * cimag(d), -h * creal(d));   /* -i (sqrt 3 / 2) (a1 - a2) */
+                    out[b] = a0 + t1;
+                    out[os + b] = t2 + t3;
+                    out[2 * os + b] = t2 - t3;
+                }
+            }
+        }
+        cplx* t = src;
+        src = dst;
+        dst = t;
+        Ns *= R;
+    }
+    if (src != x) memcpy(x, src, sizeof(cplx) * (size_t)n * B);
+}
+
+/* inverse (unnormalised) as conj(DFT(conj(x))) */
+static void bfft_inv(const bplan* p, cplx* x, cplx* y, int B) {
+    const size_t nb = (size_t)p->n * B;
+    for (size_t q = 0; q < nb; ++q) x[q] = conj(x[q]);
+    bfft(p, x, y, B);
+    for (size_t q = 0; q < nb; ++q) x[q] = conj(x[q]);
+}
+
+/* ------------------------------------------------------------------------ */
 /* Context                                                                   */
 /* ------------------------------------------------------------------------ */
 struct orc_ctx {
@@ -191,6 +302,8 @@ struct orc_ctx {
     int* kx; int* ky; int* kz;
     double* x;               /* collocation points (solver.c:1786-1823) */
     fft_plan plan;
+    bplan bp;                /* batched transform of length N (bp.ok: radix 2 / 3 / 4 factors only) */
+    cplx* ftmp;              /* c2r scratch, 3 nF (with bp.ok) */
     cplx* u_hat;             /* state, reference layout */
     cplx *rk1, *rk2, *rk3, *rk4, *rk_tmp, *w_hat;
     cplx *rk5, *rk6, *rk7, *u_new;   /* RK5CN / DP5CN only */
@@ -246,6 +359,8 @@ orc_ctx* orc_create(const orc_params* p) {
     c->x = (double*)malloc(sizeof(double) * c->N);
     init_space(c);
     plan_init(&c->plan, c->N);
+    bplan_init(&c->bp, c->N);
+    if (c->bp.ok) c->ftmp = (cplx*)malloc(sizeof(cplx) * 3 * (size_t)c->nF);
     size_t fb = sizeof(cplx) * 3 * (size_t)c->nF, rb = sizeof(double) * 3 * (size_t)c->nR;
     c->u_hat = (cplx*)calloc(1, fb);
     c->rk1 = (cplx*)calloc(1, fb);
@@ -275,6 +390,8 @@ void orc_destroy(orc_ctx* c) {
     if (!c) return;
     free(c->kx); free(c->ky); free(c->kz); free(c->x);
     plan_free(&c->plan);
+    bplan_free(&c->bp);
+    free(c->ftmp);
     free(c->u_hat); free(c->rk1); free(c->rk2); free(c->rk3); free(c->rk4);
     free(c->rk_tmp); free(c->w_hat); free(c->vel); free(c->vort); free(c->curl);
     free(c->rk5); free(c->rk6); free(c->rk7); free(c->u_new);
@@ -308,9 +425,128 @@ void orc_set_forcing_target(orc_ctx* c, double e) { c->force_target = e; }
 /* 3D transforms, batched over 3 interleaved components (replaces the FFTW   */
 /* plans of solver.c:2045-2068 with the logical size {N,N,N}, i.e. D1 fixed) */
 /* ------------------------------------------------------------------------ */
+/* y (along j at fixed i) or x (along i at fixed j) pass over blocks of
+   ORC_BCOLS contiguous columns of the C = 3 NF complex values of an (i, j)
+   row; inv selects the inverse transform */
+static void pass_xy(orc_ctx* c, const cplx* src, cplx* dst, int axis_x, int inv) {
+    const int N = c->N, C = 3 * c->NF;
+    const int nblk = (C + ORC_BCOLS - 1) / ORC_BCOLS;
+    const size_t rs = axis_x ? (size_t)N * C : (size_t)C;   /* row stride along the transformed axis */
+#pragma omp parallel
+    {
+        cplx* x = (cplx*)malloc(sizeof(cplx) * (size_t)N * ORC_BCOLS);
+        cplx* y = (cplx*)malloc(sizeof(cplx) * (size_t)N * ORC_BCOLS);
+#pragma omp for collapse(2) schedule(static)
+        for (int o = 0; o < N; ++o)
+            for (int blk = 0; blk < nblk; ++blk) {
+                const int c0 = blk * ORC_BCOLS, B = C - c0 < ORC_BCOLS ? C - c0 : ORC_BCOLS;
+                const size_t off = (axis_x ? (size_t)o * C : (size_t)o * N * C) + c0;
+                for (int r = 0; r < N; ++r) memcpy(x + (size_t)r * B, src + off + r * rs, sizeof(cplx) * B);
+                if (inv) bfft_inv(&c->bp, x, y, B);
+                else bfft(&c->bp, x, y, B);
+                for (int r = 0; r < N; ++r) memcpy(dst + off + r * rs, x + (size_t)r * B, sizeof(cplx) * B);
+            }
+        free(x);
+        free(y);
+    }
+}
+
+/* z lines of one x plane i, JB consecutive j at a time: the 3 JB real lines
+   (j, d) packed in pairs as complex lines, z = line 2q + i line 2q+1 */
+static int z_block(int N) { return N % 4 == 0 ? 4 : 2; }
+
+static void r2c_fast(orc_ctx* c, const double* real, cplx* out) {
+    const int N = c->N, NF = c->NF, JB = z_block(N), B = 3 * JB / 2;
+#pragma omp parallel
+    {
+        cplx* x = (cplx*)malloc(sizeof(cplx) * (size_t)N * B);
+        cplx* y = (cplx*)malloc(sizeof(cplx) * (size_t)N * B);
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int j0 = 0; j0 < N; j0 += JB) {
+                for (int k = 0; k < N; ++k)
+                    for (int q = 0; q < B; ++q) {
+                        const int la = 2 * q, lb = 2 * q + 1;
+                        const double va = real[3 * ((long)(i * N + j0 + la / 3) * (N + 2) + k) + la % 3];
+                        const double vb = real[3 * ((long)(i * N + j0 + lb / 3) * (N + 2) + k) + lb % 3];
+                        x[(size_t)k * B + q] = CMPLX(va, vb);
+                    }
+                bfft(&c->bp, x, y, B);
+                /* X_a[k] = (Z[k] + conj Z[N-k]) / 2, X_b[k] = (Z[k] - conj Z[N-k]) / (2 i) */
+                for (int k = 0; k < NF; ++k)
+                    for (int q = 0; q < B; ++q) {
+                        const cplx z = x[(size_t)k * B + q], zc = conj(x[(size_t)((N - k) % N) * B + q]);
+                        const cplx sa = z + zc, sb = z - zc;
+                        const int la = 2 * q, lb = 2 * q + 1;
+                        out[3 * ((long)(i * N + j0 + la / 3) * NF + k) + la % 3] = 0.5 * sa;
+                        out[3 * ((long)(i * N + j0 + lb / 3) * NF + k) + lb % 3] = CMPLX(0.5 * cimag(sb), -0.5 * creal(sb));
+                    }
+            }
+        free(x);
+        free(y);
+    }
+    pass_xy(c, out, out, 0, 0);   /* y */
+    pass_xy(c, out, out, 1, 0);   /* x */
+}
+
+static void c2r_fast(orc_ctx* c, const cplx* in, double* real) {
+    const int N = c->N, NF = c->NF, JB = z_block(N), B = 3 * JB / 2;
+    cplx* tmp = c->ftmp;     /* the input is preserved */
+    pass_xy(c, in, tmp, 1, 1);    /* x */
+    pass_xy(c, tmp, tmp, 0, 1);   /* y */
+#pragma omp parallel
+    {
+        cplx* x = (cplx*)malloc(sizeof(cplx) * (size_t)N * B);
+        cplx* y = (cplx*)malloc(sizeof(cplx) * (size_t)N * B);
+#pragma omp for collapse(2) schedule(static)
+        for (int i = 0; i < N; ++i)
+            for (int j0 = 0; j0 < N; j0 += JB) {
+                /* Z[k] = A[k] + i B[k] over the Hermitian extension of the two half lines;
+                   the imaginary parts of their kz = 0 and kz = N/2 entries are ignored */
+                for (int q = 0; q < B; ++q) {
+                    const int la = 2 * q, lb = 2 * q + 1;
+                    const cplx* ha = tmp + 3 * ((long)(i * N + j0 + la / 3) * NF) + la % 3;
+                    const cplx* hb = tmp + 3 * ((long)(i * N + j0 + lb / 3) * NF) + lb % 3;
+                    for (int k = 0; k < N; ++k) {
+                        cplx a, b;
+                        if (k == 0 || k == N / 2) {
+                            a = creal(ha[3 * k]);
+                            b = creal(hb[3 * k]);
+                        } else if (k < N / 2) {
+                            a = ha[3 * k];
+                            b = hb[3 * k];
+                        } else {
+                            a = conj(ha[3 * (N - k)]);
+                            b = conj(hb[3 * (N - k)]);
+                        }
+                        x[(size_t)k * B + q] = CMPLX(creal(a) - cimag(b), cimag(a) + creal(b));
+                    }
+                }
+                bfft_inv(&c->bp, x, y, B);
+                for (int q = 0; q < B; ++q) {
+                    const int la = 2 * q, lb = 2 * q + 1;
+                    double* ra = real + 3 * ((long)(i * N + j0 + la / 3) * (N + 2)) + la % 3;
+                    double* rb = real + 3 * ((long)(i * N + j0 + lb / 3) * (N + 2)) + lb % 3;
+                    for (int k = 0; k < N; ++k) {
+                        ra[3 * k] = creal(x[(size_t)k * B + q]);
+                        rb[3 * k] = cimag(x[(size_t)k * B + q]);
+                    }
+                    ra[3 * N] = ra[3 * (N + 1)] = 0.0;
+                    rb[3 * N] = rb[3 * (N + 1)] = 0.0;
+                }
+            }
+        free(x);
+        free(y);
+    }
+}
+
 void orc_fft_r2c(orc_ctx* c, const double* real, double* u_hat_d) {
     const int N = c->N, NF = c->NF;
     cplx* out = (cplx*)u_hat_d;
+    if (c->bp.ok) {
+        r2c_fast(c, real, out);
+        return;
+    }
     /* z: real lines -> half spectrum */
 #pragma omp parallel
     {
@@ -351,6 +587,10 @@ void orc_fft_r2c(orc_ctx* c, const double* real, double* u_hat_d) {
 void orc_fft_c2r(orc_ctx* c, const double* u_hat_d, double* real) {
     const int N = c->N, NF = c->NF;
     const cplx* in = (const cplx*)u_hat_d;
+    if (c->bp.ok) {
+        c2r_fast(c, in, real);
+        return;
+    }
     cplx* tmp = (cplx*)malloc(sizeof(cplx) * 3 * (size_t)c->nF);   /* preserve input */
 #pragma omp parallel
     {
@@ -404,6 +644,8 @@ void orc_fft_c2r(orc_ctx* c, const double* u_hat_d, double* real) {
 void orc_dealias(orc_ctx* c, double* arr_d, int array_dim) {
     const int N = c->N, NF = c->NF;
     cplx* array = (cplx*)arr_d;
+    /* modes are independent unless D2 is reproduced (its copies read other modes in order) */
+#pragma omp parallel for collapse(2) schedule(static) if (!c->p.bugcompat_dealias)
     for (int i = 0; i < N; ++i)
         for (int j = 0; j < N; ++j)
             for (int k = 0; k < NF; ++k) {
@@ -430,9 +672,9 @@ static void rhs_impl(orc_ctx* c, const cplx* u_hat, cplx* dw, int want_umax) {
             for (int k = 0; k < NF; ++k) {
                 long indx = (long)(i * N + j) * NF + k;
                 const cplx* u = u_hat + 3 * indx;
-                dw[3 * indx + 0] = I * (c->ky[j] * u[2] - c->kz[k] * u[1]);
-                dw[3 * indx + 1] = I * (c->kz[k] * u[0] - c->kx[i] * u[2]);
-                dw[3 * indx + 2] = I * (c->kx[i] * u[1] - c->ky[j] * u[0]);
+                dw[3 * indx + 0] = mul_i(c->ky[j] * u[2] - c->kz[k] * u[1]);
+                dw[3 * indx + 1] = mul_i(c->kz[k] * u[0] - c->kx[i] * u[2]);
+                dw[3 * indx + 2] = mul_i(c->kx[i] * u[1] - c->ky[j] * u[0]);
             }
     /* to real space (solver.c:656-658) */
     orc_fft_c2r(c, (const double*)dw, c->vort);
