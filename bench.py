@@ -204,7 +204,7 @@ def cpu_baseline(N: int):
     t = time.perf_counter() - t0
     return {"value": N ** 3 / t, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"one whole IF-RK4 step at {N}^3 in FP64 ({t:.1f} s, after one untimed step), "
-                      f"oracle restatement with its own mixed-radix FFT, {cores} threads"}
+                      f"oracle restatement with its own FFT (batched Stockham, no FFTW on the host), {cores} threads"}
 
 
 def run_reference(args, ws, rank):
@@ -230,7 +230,7 @@ def run_reference(args, ws, rank):
     sample = (f"each bench step = one RK4 stage at {N}^3 in FP64 (1/4 of an RK4 step: a NonlinearRHSBatch and "
               f"its stage update, every fourth with the final update and forcing); {args.steps} stages = "
               f"{args.steps / 4:g} RK4 steps in {t:.1f} s; value = N^3 x (K/4) / t; oracle restatement, "
-              f"own mixed-radix FFT, {cores} threads")
+              f"own FFT (batched Stockham, no FFTW on the host), {cores} threads")
     line = {"impl": "reference", "metric": metric(N), "value": val, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
