@@ -317,9 +317,10 @@ def run_ours(args, ws, rank, local):
                                    "alg_GBps": model_fields[p[0]] * field / (p[1] / 1e3) / 1e9 if p[0] in model_fields else None,
                                    "compulsory_GBps": (p[2] / (p[1] / 1e3) / 1e9) if p[2] else None} for p in prof}}
     step_bytes = sum(p[2] * 4 for p in prof)
-    survey_bytes = 198.0 * N ** 3 * 4
+    # the per-pass field model: 198 scalar-field passes of N^3 FP32 words per RK4 step
+    model_bytes = 198.0 * N ** 3 * 4
     roofline["step_compulsory_GB"] = step_bytes / 1e9
-    roofline["step_survey_model_GBps"] = survey_bytes / (ms_max / args.steps / 1e3) / 1e9
+    roofline["step_field_model_GBps"] = model_bytes / (ms_max / args.steps / 1e3) / 1e9
 
     e2e = None
     if not args.no_e2e:

@@ -1,6 +1,6 @@
 """Failure detection, exercised without faulting the GPU: the reference
 defines limits (MIN_STEP_SIZE, MAX_ITERS, MAX_VORT_LIM, data_types.h:130-136)
-but never checks them; this build reports failures as status codes.
+but never checks them; this library reports failures as status codes.
 
 * A bounded wait that runs out: the wait budget of the copy-fed passes (the
   z pass, and the tensor-tile x-inverse pass of variant 3) is cut to a few
