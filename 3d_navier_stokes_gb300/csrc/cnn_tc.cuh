@@ -121,27 +121,6 @@ __global__ void k_to_blocked(const float* __restrict__ u, float in_scale, uint4*
     }
 }
 
-// B operand of one layer from W[cout][cin][27] (BF16) in the shared-memory
-// order [(dx,dy) 9][n group][kchunk][8 n][8 channels], n = dz * NO + co;
-// zero padding to NO output and 8 KC input channels
-__global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cout, int cin, int KC, int NO,
-                          __nv_bfloat16* __restrict__ dst) {
-    const int NG = 3 * NO / 8;
-    const int n_all = 9 * NG * KC * 64;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_all; q += gridDim.x * blockDim.x) {
-        const int j = q % 8;
-        int r = q / 8;
-        const int n8 = r % 8;
-        r /= 8;
-        const int kc = r % KC;
-        r /= KC;
-        const int ng = r % NG;
-        const int t9 = r / NG;
-        const int n = ng * 8 + n8, dz = n / NO, co = n % NO, ci = kc * 8 + j;
-        const int t = t9 * 3 + dz;   // tap (dx+1)*9 + (dy+1)*3 + (dz+1)
-        dst[q] = (co < cout && ci < cin) ? w[((long long)co * cin + ci) * 27 + t] : __float2bfloat16(0.0f);
-    }
-}
 
 // One layer. KC: 16-byte channel chunks of the input (CIN padded to 8 KC);
 // NO: output channels per dz block (32, or 16 for the output layer);
@@ -150,7 +129,7 @@ __global__ void k_pack_tc(const __nv_bfloat16* __restrict__ w, int cout, int cin
 // [cout][D^3]; training: 2: z = out + b to zbuf (FP32 [32][D^3]) and
 // a = GELU(z) blocked and as the wg-A copy (cm) of the weight-gradient kernel;
 // 3 (the input gradient, weights packed transposed and mirrored by
-// k_pack_tc_t, no bias): d = out * GELU'(zbuf) blocked and as the wg-B copies
+// k_pack_jobs with transposed = 1, no bias): d = out * GELU'(zbuf) blocked and as the wg-B copies
 // (cm). 256 threads: thread 0 issues the copies and the MMAs, every
 // warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
 // channels [16 (w / 4), 16 (w / 4) + 16).
@@ -375,27 +354,67 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
 // copies of the activations and the wg-B copies of the gradients that those
 // kernels also write.
 
-// B operand of the input-gradient convolution of a layer with weights
-// W[cout][cin][27]: the transposed, mirrored kernel W'[ci][co][t] =
-// W[co][ci][26 - t] (input channels co in KC chunks, output channels ci < NO),
-// in k_pack_tc's shared-memory order
-__global__ void k_pack_tc_t(const __nv_bfloat16* __restrict__ w, int cout, int cin, int KC, int NO,
-                            __nv_bfloat16* __restrict__ dst) {
-    const int NG = 3 * NO / 8;
-    const int n_all = 9 * NG * KC * 64;
+
+// B operands of the layers from W[cout][cin][27] (BF16), several in one launch
+// (job blockIdx.y), in the shared-memory order [(dx,dy) 9][n group][kchunk][8 n][8
+// channels], n = dz * NO + output channel, zero padding to NO output and 8 KC input
+// channels. transposed = 0: the layer's own kernel, output channels co, input
+// channels ci; transposed = 1: the B operand of its input-gradient convolution,
+// the kernel transposed and mirrored, W'[ci][co][t] = W[co][ci][26 - t] (input
+// channels co in KC chunks, output channels ci < NO).
+struct PackJob {
+    const __nv_bfloat16* w;
+    __nv_bfloat16* dst;
+    int cout, cin, KC, NO, transposed;
+};
+struct PackJobs {
+    PackJob job[8];
+};
+__global__ void k_pack_jobs(const PackJobs jobs) {
+    const PackJob J = jobs.job[blockIdx.y];
+    const int NG = 3 * J.NO / 8;
+    const int n_all = 9 * NG * J.KC * 64;
     for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n_all; q += gridDim.x * blockDim.x) {
         const int j = q % 8;
         int r = q / 8;
         const int n8 = r % 8;
         r /= 8;
-        const int kc = r % KC;
-        r /= KC;
+        const int kc = r % J.KC;
+        r /= J.KC;
         const int ng = r % NG;
         const int t9 = r / NG;
-        const int n = ng * 8 + n8, dz = n / NO, o = n % NO, i = kc * 8 + j;
+        const int n = ng * 8 + n8, dz = n / J.NO, a = n % J.NO, b = kc * 8 + j;
         const int t = t9 * 3 + dz;
-        dst[q] = (o < cin && i < cout) ? w[((long long)i * cin + o) * 27 + (26 - t)] : __float2bfloat16(0.0f);
+        if (J.transposed)
+            J.dst[q] = (a < J.cin && b < J.cout) ? J.w[((long long)b * J.cin + a) * 27 + (26 - t)] : __float2bfloat16(0.0f);
+        else
+            J.dst[q] = (a < J.cout && b < J.cin) ? J.w[((long long)a * J.cin + b) * 27 + t] : __float2bfloat16(0.0f);
     }
+}
+
+// per-channel sums of an FP32 [nch][n] array in two fixed-order levels:
+// partial[c][blockIdx.x] over a strided share, then the partials in order
+__global__ void k_chan_partial(const float* __restrict__ x, long long n, float* __restrict__ partial) {
+    __shared__ float red[256];
+    const int c = blockIdx.y;
+    const float* xc = x + (long long)c * n;
+    float s = 0.0f;
+    for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < n; p += (long long)gridDim.x * blockDim.x)
+        s += xc[p];
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) partial[c * gridDim.x + blockIdx.x] = red[0];
+}
+__global__ void k_chan_final(const float* __restrict__ partial, int nparts, int nch, float* __restrict__ out) {
+    const int c = threadIdx.x;
+    if (c >= nch) return;
+    float s = 0.0f;
+    for (int q = 0; q < nparts; ++q) s += partial[c * nparts + q];
+    out[c] = s;
 }
 
 // FP32 velocity [3][D^3] x in_scale -> wg-A BF16 with 8 channels (3..7 zero);
@@ -430,21 +449,6 @@ __global__ void k_grad_pack(const float* __restrict__ g, uint4* __restrict__ blk
     }
 }
 
-// per-channel sums (bias gradients), one CTA per channel, fixed order
-template <typename T>
-__global__ void k_chan_sum(const T* __restrict__ x, long long D3, float* __restrict__ out) {
-    __shared__ float red[256];
-    const T* xc = x + (long long)blockIdx.x * D3;
-    float s = 0.0f;
-    for (long long p = threadIdx.x; p < D3; p += blockDim.x) s += (float)xc[p];
-    red[threadIdx.x] = s;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if (threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) out[blockIdx.x] = red[0];
-}
 
 __host__ __device__ constexpr int tc_pow2(int v) {
     int p = 32;

@@ -818,9 +818,11 @@ template <int N> struct ZPlan { using A = typename Plans<N>::A; };
 template <int N> constexpr int zline_gw() { return ZPlan<N>::A::P > 32 ? ZPlan<N>::A::P / 32 : 1; }
 template <int N> constexpr int zline_gpw() { return ZPlan<N>::A::P <= 32 ? 32 / ZPlan<N>::A::P : 1; }
 // the real Nz line as a half-length complex transform where a plan of N/2 points
-// runs on the same lanes with half the elements
+// runs on the same lanes with half the elements, and where it measured faster: one
+// line per warp at 512 and 1024 points (512^3: 1.183 -> 1.168 ms per pass; at 256
+// points, two lines per warp, 0.123 -> 0.140 ms, so not there)
 template <int N> constexpr bool zline_half_nz() {
-    if constexpr (N % 2 != 0 || N < 256 || (N & (N - 1)) != 0) {
+    if constexpr (N != 512 && N != 1024) {
         return false;
     } else {
         using HP = typename Plans<N / 2>::X;

@@ -83,6 +83,7 @@ constexpr int oW1 = 0, ob1 = oW1 + C * 3 * 27, oW2 = ob1 + C, ob2 = oW2 + C * C 
               ob3 = oW3 + C * C * 27, oW4 = ob3 + C, ob4 = oW4 + 6 * C * 27, NPARAM = ob4 + 6;
 constexpr int NPART = 256;
 constexpr int kTrainChunk = 64;   // Adam iterations queued between host checks of the losses
+constexpr int kChanParts = 32;    // CTAs per channel of the output-bias gradient sum
 // packed tensor-core B operands of the four layers (BF16 elements):
 // (KC, NO) = (2, 32), (4, 32), (4, 32), (4, 16); 9 x 3 NO x 8 KC each
 constexpr int kTcW1 = 9 * 96 * 2 * 8, kTcW2 = 9 * 96 * 4 * 8, kTcW4 = 9 * 48 * 4 * 8;
@@ -128,6 +129,7 @@ struct ns3d_les : public ns3d::LesHook {
     double* losses = nullptr;
     double* losses_host = nullptr;
     int* halt = nullptr;
+    float* chanp = nullptr;   // output-bias gradient partial sums [6][kChanParts]
     int wg_grid = 0;
     int train_path = 0;                                  // 0: tensor cores where compiled, 1: FP32 CUDA cores
     int tc_grid[3] = {0, 0, 0};                          // CTAs of the three kernel shapes
@@ -170,10 +172,12 @@ struct ns3d_les : public ns3d::LesHook {
     // B operands of the input-gradient convolutions from the current BF16 weights
     void pack_tc_t(cudaStream_t s) {
         if (!wtc_t) return;
-        using ns3d::cnn::k_pack_tc_t;
-        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW4, 6, C, 2, 32, wtc_t + oU4);
-        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW3, C, C, 4, 32, wtc_t + oU3);
-        k_pack_tc_t<<<64, 256, 0, s>>>(wb + oW2, C, C, 4, 32, wtc_t + oU2);
+        using namespace ns3d::cnn;
+        PackJobs jobs{};
+        jobs.job[0] = PackJob{wb + oW4, wtc_t + oU4, 6, C, 2, 32, 1};
+        jobs.job[1] = PackJob{wb + oW3, wtc_t + oU3, C, C, 4, 32, 1};
+        jobs.job[2] = PackJob{wb + oW2, wtc_t + oU2, C, C, 4, 32, 1};
+        k_pack_jobs<<<dim3(64, 3), 256, 0, s>>>(jobs);
     }
 
     // dW of one layer on the tensor cores, reduced into g + off (cin x cout x 27)
@@ -218,7 +222,8 @@ struct ns3d_les : public ns3d::LesHook {
         k_mse<<<NPART, 256, 0, s>>>(y, t, (float)(1.0 / s_out), gy, 6 * D3, part);
         // layer 4: d4 = dloss/dy (blocked into b0, which the forward no longer needs)
         k_grad_pack<LOGD><<<eg, 256, 0, s>>>(gy, b0, reinterpret_cast<uint4*>(d4cm));
-        k_chan_sum<float><<<6, 256, 0, s>>>(gy, D3, g + ob4);
+        k_chan_partial<<<dim3(kChanParts, 6), 256, 0, s>>>(gy, D3, chanp);
+        k_chan_final<<<1, 32, 0, s>>>(chanp, kChanParts, 6, g + ob4);
         wgrad_tc<32, 16, LOGD>(a3cm, d4cm, C, 6, oW4, -1, s);
         k_conv3_tc<2, 32, LOGD, 3><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
             b0, WT + oU4 / 8, zeros, b3, C, 1.f, dstat, z3, d3cm);
@@ -258,11 +263,13 @@ struct ns3d_les : public ns3d::LesHook {
     // B operands of the tensor-core layers from the current BF16 weights
     void pack_tc(cudaStream_t s) {
         if (!tc()) return;
-        using ns3d::cnn::k_pack_tc;
-        k_pack_tc<<<64, 256, 0, s>>>(wb + oW1, C, 3, 2, 32, wtc + oT1);
-        k_pack_tc<<<64, 256, 0, s>>>(wb + oW2, C, C, 4, 32, wtc + oT2);
-        k_pack_tc<<<64, 256, 0, s>>>(wb + oW3, C, C, 4, 32, wtc + oT3);
-        k_pack_tc<<<64, 256, 0, s>>>(wb + oW4, 6, C, 4, 16, wtc + oT4);
+        using namespace ns3d::cnn;
+        PackJobs jobs{};
+        jobs.job[0] = PackJob{wb + oW1, wtc + oT1, C, 3, 2, 32, 0};
+        jobs.job[1] = PackJob{wb + oW2, wtc + oT2, C, C, 4, 32, 0};
+        jobs.job[2] = PackJob{wb + oW3, wtc + oT3, C, C, 4, 32, 0};
+        jobs.job[3] = PackJob{wb + oW4, wtc + oT4, 6, C, 4, 16, 0};
+        k_pack_jobs<<<dim3(64, 4), 256, 0, s>>>(jobs);
     }
 
     // tensor-core inference: four implicit-GEMM convolutions on blocked BF16 activations
@@ -303,7 +310,7 @@ struct ns3d_les : public ns3d::LesHook {
                         (void*)z2, (void*)z3, (void*)y, (void*)gy, (void*)gz3, (void*)gz2, (void*)gz1, (void*)io_u,
                         (void*)io_t, (void*)part, (void*)wtc, (void*)act0, (void*)act1, (void*)act2, (void*)act3,
                         (void*)dstat, (void*)wtc_t, (void*)a0cm, (void*)a1cm, (void*)a2cm, (void*)a3cm, (void*)d1cm,
-                        (void*)d2cm, (void*)d3cm, (void*)d4cm, (void*)wpart, (void*)zeros, (void*)losses, (void*)halt})
+                        (void*)d2cm, (void*)d3cm, (void*)d4cm, (void*)wpart, (void*)zeros, (void*)losses, (void*)halt, (void*)chanp})
             if (q) cudaFree(q);
         if (part_host) cudaFreeHost(part_host);
         if (losses_host) cudaFreeHost(losses_host);
@@ -392,6 +399,7 @@ ns3d_status ns3d_les_create(int Nc, int capacity, uint64_t seed, ns3d_les** out)
         cudaMalloc(&l->losses, sizeof(double) * kTrainChunk) != cudaSuccess ||
         cudaMallocHost(&l->losses_host, sizeof(double) * kTrainChunk) != cudaSuccess ||
         cudaMalloc(&l->halt, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&l->chanp, sizeof(float) * 6 * kChanParts) != cudaSuccess ||
         (capacity > 0 && (cudaMalloc(&l->data_u, f * 3 * l->D3 * capacity) != cudaSuccess ||
                           cudaMalloc(&l->data_t, f * 6 * l->D3 * capacity) != cudaSuccess))) {
         delete l;
