@@ -397,7 +397,8 @@ template <typename T, int N, int V>
 constexpr size_t xinv_tma_smem() { return sizeof(cx<T>) * (size_t)N * xtma_tile<T, N, V>() * 3 + 16; }
 template <typename T, int N, int V>
 constexpr bool xinv_tma_ok() {
-    return sizeof(T) == 4 && V == 3 && N % 16 == 0 && N >= 48 && xinv_tma_smem<T, N, V>() <= 232448 &&
+    // not at 1024^3 (8-pencil tiles, 64-byte boxes): 5.17 ms per pass against 4.30 ms for k_xinv
+    return sizeof(T) == 4 && V == 3 && N % 16 == 0 && N >= 48 && N <= 512 && xinv_tma_smem<T, N, V>() <= 232448 &&
            (2 * xtma_tile<T, N, V>() * sizeof(T)) % 16 == 0;
 }
 
@@ -817,12 +818,13 @@ constexpr int ZLINE_WARPS = 4;
 template <int N> struct ZPlan { using A = typename Plans<N>::A; };
 template <int N> constexpr int zline_gw() { return ZPlan<N>::A::P > 32 ? ZPlan<N>::A::P / 32 : 1; }
 template <int N> constexpr int zline_gpw() { return ZPlan<N>::A::P <= 32 ? 32 / ZPlan<N>::A::P : 1; }
-// the real Nz line as a half-length complex transform where a plan of N/2 points
-// runs on the same lanes with half the elements, and where it measured faster: one
-// line per warp at 512 and 1024 points (512^3: 1.183 -> 1.168 ms per pass; at 256
-// points, two lines per warp, 0.123 -> 0.140 ms, so not there)
+// the real Nz line as a half-length complex transform (a plan of N/2 points on the
+// same lanes with half the elements) where it measured faster: the 512-point lines
+// of one warp (1.183 -> 1.168 ms per pass at 512^3). Slower elsewhere: 256 points,
+// two lines per warp, 0.123 -> 0.140 ms; 1024 points, two warps per line, 10.86 ->
+// 11.57 ms.
 template <int N> constexpr bool zline_half_nz() {
-    if constexpr (N != 512 && N != 1024) {
+    if constexpr (N != 512) {
         return false;
     } else {
         using HP = typename Plans<N / 2>::X;
