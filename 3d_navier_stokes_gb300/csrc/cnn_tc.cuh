@@ -55,6 +55,7 @@ using tc::tc_fence_before;
 using tc::tmem_alloc;
 using tc::tmem_dealloc;
 using tc::tmem_ld16;
+using tc::tmem_ld8;
 using tc::tmem_relinquish;
 using tc::tmem_wait_ld;
 
@@ -130,13 +131,14 @@ __global__ void k_to_blocked(const float* __restrict__ u, float in_scale, uint4*
 // a = GELU(z) blocked and as the wg-A copy (cm) of the weight-gradient kernel;
 // 3 (the input gradient, weights packed transposed and mirrored by
 // k_pack_jobs with transposed = 1, no bias): d = out * GELU'(zbuf) blocked and as the wg-B copies
-// (cm). 256 threads: thread 0 issues the copies and the MMAs, every
+// (cm). 512 threads: thread 0 issues the copies and the MMAs, every
 // warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
-// channels [16 (w / 4), 16 (w / 4) + 16).
-constexpr int kTcThreads = 256;
+// channels [8 (w / 4), 8 (w / 4) + 8).
+constexpr int kConvThreads = 512;
+constexpr int kTcThreads = 256;   // the weight-gradient kernel
 
 template <int KC, int NO, int LOGD, int OUT_MODE>
-__global__ void __launch_bounds__(kTcThreads, 1)
+__global__ void __launch_bounds__(kConvThreads, 1)
 k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const float* __restrict__ bias,
            void* __restrict__ out, int cout, float out_scale, int* __restrict__ status,
            float* __restrict__ zbuf = nullptr, __nv_bfloat16* __restrict__ cm = nullptr) {
@@ -159,7 +161,7 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
     __shared__ int s_ok;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    for (uint32_t q = tid; q < b_bytes / 16; q += kTcThreads) reinterpret_cast<uint4*>(sB)[q] = wpk[q];
+    for (uint32_t q = tid; q < b_bytes / 16; q += kConvThreads) reinterpret_cast<uint4*>(sB)[q] = wpk[q];
     fence_proxy_async_smem();   // B (generic stores) -> visible to the tensor cores
     if (tid == 0) {
         for (int b = 0; b < 2; ++b) {
@@ -249,22 +251,22 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
         tc_fence_after();
         // ---- epilogue of this tile
         const int x = tile / tiles_per_x, y0 = (tile % tiles_per_x) * R;
-        const int quarter = warp & 3, half = warp >> 2;
+        const int quarter = warp & 3, part = warp >> 2;   // lane quarter, 8-channel group
         const int m = quarter * 32 + lane;
-        const bool active = (NO == 32) || half == 0;
-        const uint32_t tl = tmem + 128u * b + ((uint32_t)(quarter * 32) << 16) + 16u * half;
-        uint32_t gm[16], g0[16], gp[16];
+        const bool active = (NO == 32) || part < 2;
+        const uint32_t tl = tmem + 128u * b + ((uint32_t)(quarter * 32) << 16) + 8u * part;
+        uint32_t gm[8], g0[8], gp[8];
         if (active) {
-            tmem_ld16(tl, gm);
-            tmem_ld16(tl + NO, g0);
-            tmem_ld16(tl + 2 * NO, gp);
+            tmem_ld8(tl, gm);
+            tmem_ld8(tl + NO, g0);
+            tmem_ld8(tl + 2 * NO, gp);
             tmem_wait_ld(gm);
             tmem_wait_ld(g0);
             tmem_wait_ld(gp);
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                sX[(16 * half + j) * 128 + m] = __uint_as_float(gm[j]);
-                sX[(NO + 16 * half + j) * 128 + m] = __uint_as_float(gp[j]);
+            for (int j = 0; j < 8; ++j) {
+                sX[(8 * part + j) * 128 + m] = __uint_as_float(gm[j]);
+                sX[(NO + 8 * part + j) * 128 + m] = __uint_as_float(gp[j]);
             }
         }
         tc_fence_before();
@@ -272,28 +274,24 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
         if (active) {
             const int line = m & ~(D - 1), zz = m & (D - 1), yy = y0 + (m >> LOGD);
             const int left = line | ((zz - 1) & (D - 1)), right = line | ((zz + 1) & (D - 1));
-            float v[16];
+            float v[8];
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-                const int co = 16 * half + j;
+            for (int j = 0; j < 8; ++j) {
+                const int co = 8 * part + j;
                 v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] +
                        bias[co < cout ? co : 0];
             }
             if constexpr (OUT_MODE == 0) {
                 uint4* dst = reinterpret_cast<uint4*>(out);
-#pragma unroll
-                for (int q = 0; q < 2; ++q)
-                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] =
-                        make_uint4(pack_bf16x2(gelu_tc(v[q * 8 + 0]), gelu_tc(v[q * 8 + 1])),
-                                   pack_bf16x2(gelu_tc(v[q * 8 + 2]), gelu_tc(v[q * 8 + 3])),
-                                   pack_bf16x2(gelu_tc(v[q * 8 + 4]), gelu_tc(v[q * 8 + 5])),
-                                   pack_bf16x2(gelu_tc(v[q * 8 + 6]), gelu_tc(v[q * 8 + 7])));
+                dst[blk_index<LOGD, 4>(x, yy, zz, part)] =
+                    make_uint4(pack_bf16x2(gelu_tc(v[0]), gelu_tc(v[1])), pack_bf16x2(gelu_tc(v[2]), gelu_tc(v[3])),
+                               pack_bf16x2(gelu_tc(v[4]), gelu_tc(v[5])), pack_bf16x2(gelu_tc(v[6]), gelu_tc(v[7])));
             } else if constexpr (OUT_MODE == 2 || OUT_MODE == 3) {
                 const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
-                float o[16];
+                float o[8];
 #pragma unroll
-                for (int j = 0; j < 16; ++j) {
-                    const long long qi = (long long)(16 * half + j) * D3 + p;
+                for (int j = 0; j < 8; ++j) {
+                    const long long qi = (long long)(8 * part + j) * D3 + p;
                     if constexpr (OUT_MODE == 2) {
                         zbuf[qi] = v[j];
                         o[j] = gelu_tc(v[j]);
@@ -303,23 +301,19 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
                 }
                 uint4* dst = reinterpret_cast<uint4*>(out);
                 uint4* wg = reinterpret_cast<uint4*>(cm);
-#pragma unroll
-                for (int q = 0; q < 2; ++q) {
-                    const uint4 pk =
-                        make_uint4(pack_bf16x2(o[q * 8 + 0], o[q * 8 + 1]), pack_bf16x2(o[q * 8 + 2], o[q * 8 + 3]),
-                                   pack_bf16x2(o[q * 8 + 4], o[q * 8 + 5]), pack_bf16x2(o[q * 8 + 6], o[q * 8 + 7]));
-                    dst[blk_index<LOGD, 4>(x, yy, zz, 2 * half + q)] = pk;
-                    if constexpr (OUT_MODE == 2)
-                        wg[wga_index<LOGD, 32>(x, yy, 2 * half + q, zz)] = pk;
-                    else
-                        wgb_store<LOGD, 32>(wg, x, yy, 2 * half + q, zz, pk);
-                }
+                const uint4 pk = make_uint4(pack_bf16x2(o[0], o[1]), pack_bf16x2(o[2], o[3]), pack_bf16x2(o[4], o[5]),
+                                            pack_bf16x2(o[6], o[7]));
+                dst[blk_index<LOGD, 4>(x, yy, zz, part)] = pk;
+                if constexpr (OUT_MODE == 2)
+                    wg[wga_index<LOGD, 32>(x, yy, part, zz)] = pk;
+                else
+                    wgb_store<LOGD, 32>(wg, x, yy, part, zz, pk);
             } else {
                 float* dst = reinterpret_cast<float*>(out);
                 const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
 #pragma unroll
-                for (int j = 0; j < 16; ++j)
-                    if (j < cout) dst[j * D3 + p] = v[j] * out_scale;
+                for (int j = 0; j < 8; ++j)
+                    if (8 * part + j < cout) dst[(8 * part + j) * D3 + p] = v[j] * out_scale;
             }
         }
         // the exchange buffer and this accumulator are free before their next use

@@ -211,13 +211,13 @@ struct ns3d_les : public ns3d::LesHook {
         const unsigned eg = (unsigned)((D3 + 255) / 256);
         k_to_blocked<LOGD><<<eg, 256, 0, s>>>(u, is, b0);
         k_to_wga<LOGD><<<eg, 256, 0, s>>>(u, is, reinterpret_cast<uint4*>(a0cm));
-        k_conv3_tc<2, 32, LOGD, 2><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+        k_conv3_tc<2, 32, LOGD, 2><<<tc_grid[0], kConvThreads, tc_smem_bytes(2, 32, D), s>>>(
             b0, W + oT1 / 8, w + ob1, b1, C, 1.f, dstat, z1, a1cm);
-        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             b1, W + oT2 / 8, w + ob2, b2, C, 1.f, dstat, z2, a2cm);
-        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 2><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             b2, W + oT3 / 8, w + ob3, b3, C, 1.f, dstat, z3, a3cm);
-        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kTcThreads, tc_smem_bytes(4, 16, D), s>>>(
+        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kConvThreads, tc_smem_bytes(4, 16, D), s>>>(
             b3, W + oT4 / 8, w + ob4, y, 6, 1.f, dstat);
         k_mse<<<NPART, 256, 0, s>>>(y, t, (float)(1.0 / s_out), gy, 6 * D3, part);
         // layer 4: d4 = dloss/dy (blocked into b0, which the forward no longer needs)
@@ -225,15 +225,15 @@ struct ns3d_les : public ns3d::LesHook {
         k_chan_partial<<<dim3(kChanParts, 6), 256, 0, s>>>(gy, D3, chanp);
         k_chan_final<<<1, 32, 0, s>>>(chanp, kChanParts, 6, g + ob4);
         wgrad_tc<32, 16, LOGD>(a3cm, d4cm, C, 6, oW4, -1, s);
-        k_conv3_tc<2, 32, LOGD, 3><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+        k_conv3_tc<2, 32, LOGD, 3><<<tc_grid[0], kConvThreads, tc_smem_bytes(2, 32, D), s>>>(
             b0, WT + oU4 / 8, zeros, b3, C, 1.f, dstat, z3, d3cm);
         // layer 3
         wgrad_tc<32, 32, LOGD>(a2cm, d3cm, C, C, oW3, ob3, s);
-        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             b3, WT + oU3 / 8, zeros, b2, C, 1.f, dstat, z2, d2cm);
         // layer 2
         wgrad_tc<32, 32, LOGD>(a1cm, d2cm, C, C, oW2, ob2, s);
-        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 3><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             b2, WT + oU2 / 8, zeros, b1, C, 1.f, dstat, z1, d1cm);
         // layer 1
         wgrad_tc<8, 32, LOGD>(a0cm, d1cm, 3, C, oW1, ob1, s);
@@ -283,13 +283,13 @@ struct ns3d_les : public ns3d::LesHook {
         uint4* a2 = reinterpret_cast<uint4*>(act2);
         uint4* a3 = reinterpret_cast<uint4*>(act3);
         k_to_blocked<LOGD><<<(unsigned)((D3 + 255) / 256), 256, 0, s>>>(u, in_scale, a0);
-        k_conv3_tc<2, 32, LOGD, 0><<<tc_grid[0], kTcThreads, tc_smem_bytes(2, 32, D), s>>>(
+        k_conv3_tc<2, 32, LOGD, 0><<<tc_grid[0], kConvThreads, tc_smem_bytes(2, 32, D), s>>>(
             a0, W + oT1 / 8, w + ob1, a1, C, 1.f, dstat);
-        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             a1, W + oT2 / 8, w + ob2, a2, C, 1.f, dstat);
-        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kTcThreads, tc_smem_bytes(4, 32, D), s>>>(
+        k_conv3_tc<4, 32, LOGD, 0><<<tc_grid[1], kConvThreads, tc_smem_bytes(4, 32, D), s>>>(
             a2, W + oT3 / 8, w + ob3, a3, C, 1.f, dstat);
-        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kTcThreads, tc_smem_bytes(4, 16, D), s>>>(
+        k_conv3_tc<4, 16, LOGD, 1><<<tc_grid[2], kConvThreads, tc_smem_bytes(4, 16, D), s>>>(
             a3, W + oT4 / 8, w + ob4, tau, 6, out_scale, dstat);
     }
     void infer_tc(const float* u, float* tau, float in_scale, float out_scale, cudaStream_t s) {
@@ -330,7 +330,7 @@ static ns3d_status les_tc_setup_d(ns3d_les* l, int nsm) {
         if (cudaFuncSetAttribute(fns[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm[k]) != cudaSuccess)
             return NS3D_ERR_CUDA;
         int per = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fns[k], kTcThreads, sm[k]) != cudaSuccess || per < 1)
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, fns[k], kConvThreads, sm[k]) != cudaSuccess || per < 1)
             return NS3D_ERR_CUDA;
         l->tc_grid[k] = per * nsm < ntiles ? per * nsm : ntiles;
     }
