@@ -74,7 +74,7 @@ __host__ __device__ constexpr uint32_t tc_a_bytes(int KC, int D) {
 __host__ __device__ constexpr uint32_t tc_b_bytes(int KC, int NO) { return 9u * 3u * (uint32_t)NO * (uint32_t)KC * 16u; }
 __host__ __device__ constexpr uint32_t tc_x_bytes(int NO) { return 2u * (uint32_t)NO * 128u * 4u; }
 __host__ __device__ constexpr uint32_t tc_smem_bytes(int KC, int NO, int D) {
-    return tc_b_bytes(KC, NO) + 2u * tc_a_bytes(KC, D) + tc_x_bytes(NO) + 48u;
+    return tc_b_bytes(KC, NO) + 2u * tc_a_bytes(KC, D) + tc_x_bytes(NO) + 64u;
 }
 
 // blocked activation index (in 16-byte units) of point (x, y, z), chunk kc
@@ -131,11 +131,30 @@ __global__ void k_to_blocked(const float* __restrict__ u, float in_scale, uint4*
 // a = GELU(z) blocked and as the wg-A copy (cm) of the weight-gradient kernel;
 // 3 (the input gradient, weights packed transposed and mirrored by
 // k_pack_jobs with transposed = 1, no bias): d = out * GELU'(zbuf) blocked and as the wg-B copies
-// (cm). 512 threads: thread 0 issues the copies and the MMAs, every
-// warp w runs the epilogue of tensor-memory lane quarter w % 4 and output
-// channels [8 (w / 4), 8 (w / 4) + 8).
-constexpr int kConvThreads = 512;
-constexpr int kTcThreads = 256;   // the weight-gradient kernel
+// (cm). Warp-specialised, 17 warps: lane 0 of warp 16 (the producer) issues the
+// copies and the MMAs; warps 0..15 (the epilogue) each take tensor-memory lane
+// quarter w % 4 and output channels [8 (w / 4), 8 (w / 4) + 8). Handoffs run on
+// mbarriers only: full[b] (the copies of A buffer b landed), done[b] (the MMAs
+// into accumulator b completed, also freeing A buffer b), aempty[b] (the 16
+// epilogue warps have read accumulator b); the epilogue warps synchronise among
+// themselves on a named barrier, so the producer keeps the MMAs of tile i + 1
+// running while tile i's epilogue runs.
+constexpr int kConvWarps = 16;                        // epilogue warps
+constexpr int kConvThreads = 32 * (kConvWarps + 1);   // and the producer warp
+constexpr int kTcThreads = 256;                       // the weight-gradient kernel
+
+// the epilogue warps' named barrier 1 (512 threads), and the same with an AND
+// of a predicate across them
+__device__ __forceinline__ void epi_sync() { asm volatile("bar.sync 1, %0;" ::"n"(32 * kConvWarps) : "memory"); }
+__device__ __forceinline__ bool epi_sync_and(bool v) {
+    uint32_t r;
+    asm volatile(
+        "{\n .reg .pred p, q;\n setp.ne.u32 q, %1, 0;\n bar.red.and.pred p, 1, %2, q;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(r)
+        : "r"((uint32_t)v), "n"(32 * kConvWarps)
+        : "memory");
+    return r != 0;
+}
 
 template <int KC, int NO, int LOGD, int OUT_MODE>
 __global__ void __launch_bounds__(kConvThreads, 1)
@@ -155,11 +174,13 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
     unsigned char* sB = smem;
     unsigned char* sA = smem + b_bytes;                                        // two buffers
     float* sX = reinterpret_cast<float*>(sA + 2 * a_bytes);                    // [2][NO][128]
-    uint64_t* done = reinterpret_cast<uint64_t*>(sA + 2 * a_bytes + tc_x_bytes(NO));   // MMAs of buffer b done
+    uint64_t* done = reinterpret_cast<uint64_t*>(sA + 2 * a_bytes + tc_x_bytes(NO));   // MMAs into accumulator b done
     uint64_t* full = done + 2;                                                 // copies into buffer b landed
-    uint32_t* holder = reinterpret_cast<uint32_t*>(full + 2);
-    __shared__ int s_ok;
+    uint64_t* aempty = full + 2;                                               // accumulator b read by the epilogue
+    uint32_t* holder = reinterpret_cast<uint32_t*>(aempty + 2);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int first = blockIdx.x, stride = gridDim.x;
+    const int nmine = first < ntiles ? (ntiles - first + stride - 1) / stride : 0;
 
     for (uint32_t q = tid; q < b_bytes / 16; q += kConvThreads) reinterpret_cast<uint4*>(sB)[q] = wpk[q];
     fence_proxy_async_smem();   // B (generic stores) -> visible to the tensor cores
@@ -167,9 +188,9 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
         for (int b = 0; b < 2; ++b) {
             mbar_init(&done[b], 1);
             mbar_init(&full[b], 1);
+            mbar_init(&aempty[b], kConvWarps);
         }
         fence_barrier_init();
-        s_ok = 1;
     }
     if (warp == 0) {
         tmem_alloc(holder, kTcTmemCols);
@@ -179,154 +200,160 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = *holder;
-    const uint32_t sA_u = smem_u32(sA), sB_u = smem_u32(sB);
-    // thread 0 state
-    uint32_t ph_done[2] = {0u, 0u}, ph_full[2] = {0u, 0u};
-    bool mma_pending[2] = {false, false}, copy_pending[2] = {false, false};
-    bool ok = true;
 
-    // thread 0: the halo block of tile t into buffer b: 3 (R+2) line copies
-    auto load = [&](int t, int b) {
-        const int x = t / tiles_per_x, y0 = (t % tiles_per_x) * R;
-        mbar_arrive_expect_tx(&full[b], a_bytes);
+    if (warp == kConvWarps) {
+        // ------------------------------------------------------------ producer
+        if (lane == 0) {
+            const uint32_t sA_u = smem_u32(sA), sB_u = smem_u32(sB);
+            uint32_t ph_full = 0u, ph_done = 0u, ph_empty = 0u;   // bit b: parity of the next completion
+            uint32_t pend_copy = 0u, pend_mma = 0u;               // bit b: in flight
+            bool ok = true;
+            // the halo block of tile t into buffer b: 3 (R+2) line copies
+            auto load = [&](int t, int b) {
+                const int x = t / tiles_per_x, y0 = (t % tiles_per_x) * R;
+                mbar_arrive_expect_tx(&full[b], a_bytes);
 #pragma unroll 1
-        for (int l = 0; l < 3 * rows; ++l) {
-            const int xp = l / rows, yr = l % rows;
-            const int gx = (x + xp - 1) & (D - 1), gy = (y0 + yr - 1) & (D - 1);
-            bulk_g2s(sA + b * a_bytes + l * line_bytes, in + (((long long)gx << LOGD) + gy) * (D * KC), line_bytes,
-                     &full[b]);
-        }
-        copy_pending[b] = true;
-    };
-    // thread 0: wait for buffer b, then its 9 x KC/2 MMAs into accumulator b
-    auto issue = [&](int b) {
-        ok = ok && mbar_wait(&full[b], ph_full[b]);
-        ph_full[b] ^= 1u;
-        copy_pending[b] = false;
-        if (!ok) return;
-        const uint32_t a_base = sA_u + b * a_bytes, d = tmem + 128u * b;
-        uint32_t acc = 0;
+                for (int l = 0; l < 3 * rows; ++l) {
+                    const int xp = l / rows, yr = l % rows;
+                    const int gx = (x + xp - 1) & (D - 1), gy = (y0 + yr - 1) & (D - 1);
+                    bulk_g2s(sA + b * a_bytes + l * line_bytes, in + (((long long)gx << LOGD) + gy) * (D * KC),
+                             line_bytes, &full[b]);
+                }
+                pend_copy |= 1u << b;
+            };
+            if (nmine > 0) load(first, 0);
+            if (nmine > 1) load(first + stride, 1);
 #pragma unroll 1
-        for (int t9 = 0; t9 < 9; ++t9) {
-            const int dx = t9 / 3, dy = t9 % 3;   // offsets + 1
-            const uint32_t a0 = a_base + ((dx * rows + dy) * ZG) * KC * 128;
-            const uint32_t b0 = sB_u + (uint32_t)(t9 * (NB / 8) * KC) * 128;
+            for (int i = 0; i < nmine; ++i) {
+                const int b = i & 1;
+                ok = mbar_wait(&full[b], (ph_full >> b) & 1u);
+                if (!ok) break;
+                ph_full ^= 1u << b;
+                pend_copy &= ~(1u << b);
+                if (i >= 2) {   // the epilogue of tile i - 2 has read accumulator b
+                    ok = mbar_wait(&aempty[b], (ph_empty >> b) & 1u);
+                    if (!ok) break;
+                    ph_empty ^= 1u << b;
+                }
+                tc_fence_after();
+                const uint32_t a_base = sA_u + b * a_bytes, d = tmem + 128u * b;
+                uint32_t acc = 0;
+#pragma unroll 1
+                for (int t9 = 0; t9 < 9; ++t9) {
+                    const int dx = t9 / 3, dy = t9 % 3;   // offsets + 1
+                    const uint32_t a0 = a_base + ((dx * rows + dy) * ZG) * KC * 128;
+                    const uint32_t b0 = sB_u + (uint32_t)(t9 * (NB / 8) * KC) * 128;
 #pragma unroll
-            for (int ks = 0; ks < KC / 2; ++ks) {
-                mma_bf16(d, smem_desc(a0 + ks * 256, 128, KC * 128), smem_desc(b0 + ks * 256, 128, KC * 128), idesc,
-                         acc);
-                acc = 1;
+                    for (int ks = 0; ks < KC / 2; ++ks) {
+                        mma_bf16(d, smem_desc(a0 + ks * 256, 128, KC * 128), smem_desc(b0 + ks * 256, 128, KC * 128),
+                                 idesc, acc);
+                        acc = 1;
+                    }
+                }
+                mma_commit(&done[b]);
+                pend_mma |= 1u << b;
+                // those MMAs read A buffer b: refill it with tile i + 2 once they are done
+                if (i + 2 < nmine) {
+                    ok = mbar_wait(&done[b], (ph_done >> b) & 1u);
+                    if (!ok) break;
+                    ph_done ^= 1u << b;
+                    pend_mma &= ~(1u << b);
+                    load(first + (i + 2) * stride, b);
+                }
+            }
+            if (!ok) atomicExch(status, kStatusTimeout);
+            // the copies and MMAs still in flight complete before the CTA exits
+            for (int b = 0; b < 2; ++b) {
+                if (pend_copy & (1u << b)) (void)mbar_wait(&full[b], (ph_full >> b) & 1u);
+                if (pend_mma & (1u << b)) (void)mbar_wait(&done[b], (ph_done >> b) & 1u);
             }
         }
-        mma_commit(&done[b]);
-        mma_pending[b] = true;
-    };
-
-    // tile i lives in buffer and accumulator i % 2; its copies are issued one
-    // iteration ahead, as soon as the MMAs of tile i - 2 have released the buffer
-    int tile = blockIdx.x;
-    if (tid == 0) {
-        if (tile < ntiles) load(tile, 0);
-        if (tile + (int)gridDim.x < ntiles) load(tile + gridDim.x, 1);
-        if (tile < ntiles) issue(0);
-    }
-    for (int it = 0; tile < ntiles; ++it, tile += gridDim.x) {
-        const int b = it & 1, nb = b ^ 1;
-        const int next = tile + gridDim.x, next2 = next + gridDim.x;
-        if (tid == 0) {
-            if (ok) ok = mbar_wait(&done[b], ph_done[b]);
-            ph_done[b] ^= 1u;
-            mma_pending[b] = false;
-            // buffer b is free again; accumulator nb was read by the previous epilogue
-            if (ok && next2 < ntiles) load(next2, b);
-            if (ok && next < ntiles) issue(nb);
-            if (!ok) {
-                atomicExch(status, kStatusTimeout);
-                s_ok = 0;
-            }
-        }
-        __syncwarp();
-        __syncthreads();
-        if (!s_ok) break;
-        tc_fence_after();
-        // ---- epilogue of this tile
-        const int x = tile / tiles_per_x, y0 = (tile % tiles_per_x) * R;
+    } else {
+        // ------------------------------------------------------------ epilogue warps
         const int quarter = warp & 3, part = warp >> 2;   // lane quarter, 8-channel group
         const int m = quarter * 32 + lane;
         const bool active = (NO == 32) || part < 2;
-        const uint32_t tl = tmem + 128u * b + ((uint32_t)(quarter * 32) << 16) + 8u * part;
-        uint32_t gm[8], g0[8], gp[8];
-        if (active) {
-            tmem_ld8(tl, gm);
-            tmem_ld8(tl + NO, g0);
-            tmem_ld8(tl + 2 * NO, gp);
-            tmem_wait_ld(gm);
-            tmem_wait_ld(g0);
-            tmem_wait_ld(gp);
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                sX[(8 * part + j) * 128 + m] = __uint_as_float(gm[j]);
-                sX[(NO + 8 * part + j) * 128 + m] = __uint_as_float(gp[j]);
+        uint32_t ph_done = 0u;
+#pragma unroll 1
+        for (int i = 0; i < nmine; ++i) {
+            const int b = i & 1, tile = first + i * stride;
+            // tile i's MMAs are done (every epilogue thread waits; all agree on the
+            // outcome); this barrier also ends every read of sX for tile i - 1
+            const bool got = mbar_wait(&done[b], (ph_done >> b) & 1u);
+            if (!epi_sync_and(got)) {
+                if (tid == 0) atomicExch(status, kStatusTimeout);
+                break;
             }
-        }
-        tc_fence_before();
-        __syncthreads();
-        if (active) {
-            const int line = m & ~(D - 1), zz = m & (D - 1), yy = y0 + (m >> LOGD);
-            const int left = line | ((zz - 1) & (D - 1)), right = line | ((zz + 1) & (D - 1));
-            float v[8];
-#pragma unroll
-            for (int j = 0; j < 8; ++j) {
-                const int co = 8 * part + j;
-                v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] +
-                       bias[co < cout ? co : 0];
+            ph_done ^= 1u << b;
+            tc_fence_after();
+            const int x = tile / tiles_per_x, y0 = (tile % tiles_per_x) * R;
+            const uint32_t tl = tmem + 128u * b + ((uint32_t)(quarter * 32) << 16) + 8u * part;
+            uint32_t gm[8], g0[8], gp[8];
+            if (active) {
+                tmem_ld8(tl, gm);
+                tmem_ld8(tl + NO, g0);
+                tmem_ld8(tl + 2 * NO, gp);
+                tmem_wait_ld(gm);
+                tmem_wait_ld(g0);
+                tmem_wait_ld(gp);
             }
-            if constexpr (OUT_MODE == 0) {
-                uint4* dst = reinterpret_cast<uint4*>(out);
-                dst[blk_index<LOGD, 4>(x, yy, zz, part)] =
-                    make_uint4(pack_bf16x2(gelu_tc(v[0]), gelu_tc(v[1])), pack_bf16x2(gelu_tc(v[2]), gelu_tc(v[3])),
-                               pack_bf16x2(gelu_tc(v[4]), gelu_tc(v[5])), pack_bf16x2(gelu_tc(v[6]), gelu_tc(v[7])));
-            } else if constexpr (OUT_MODE == 2 || OUT_MODE == 3) {
-                const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
-                float o[8];
+            // accumulator b may be overwritten (the MMAs of tile i + 2)
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&aempty[b]);
+            if (active) {
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
-                    const long long qi = (long long)(8 * part + j) * D3 + p;
-                    if constexpr (OUT_MODE == 2) {
-                        zbuf[qi] = v[j];
-                        o[j] = gelu_tc(v[j]);
-                    } else {
-                        o[j] = v[j] * gelu_grad_tc(zbuf[qi]);
-                    }
+                    sX[(8 * part + j) * 128 + m] = __uint_as_float(gm[j]);
+                    sX[(NO + 8 * part + j) * 128 + m] = __uint_as_float(gp[j]);
                 }
-                uint4* dst = reinterpret_cast<uint4*>(out);
-                uint4* wg = reinterpret_cast<uint4*>(cm);
-                const uint4 pk = make_uint4(pack_bf16x2(o[0], o[1]), pack_bf16x2(o[2], o[3]), pack_bf16x2(o[4], o[5]),
-                                            pack_bf16x2(o[6], o[7]));
-                dst[blk_index<LOGD, 4>(x, yy, zz, part)] = pk;
-                if constexpr (OUT_MODE == 2)
-                    wg[wga_index<LOGD, 32>(x, yy, part, zz)] = pk;
-                else
-                    wgb_store<LOGD, 32>(wg, x, yy, part, zz, pk);
-            } else {
-                float* dst = reinterpret_cast<float*>(out);
-                const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
-#pragma unroll
-                for (int j = 0; j < 8; ++j)
-                    if (8 * part + j < cout) dst[(8 * part + j) * D3 + p] = v[j] * out_scale;
             }
-        }
-        // the exchange buffer and this accumulator are free before their next use
-        tc_fence_before();
-        __syncthreads();
-        tc_fence_after();
-    }
-    // after a failed wait: one more bounded wait for the copies and MMAs in flight
-    if (tid == 0) {
+            epi_sync();
+            if (active) {
+                const int line = m & ~(D - 1), zz = m & (D - 1), yy = y0 + (m >> LOGD);
+                const int left = line | ((zz - 1) & (D - 1)), right = line | ((zz + 1) & (D - 1));
+                float v[8];
 #pragma unroll
-        for (int b = 0; b < 2; ++b) {
-            if (copy_pending[b]) mbar_wait(&full[b], ph_full[b]);
-            if (mma_pending[b]) mbar_wait(&done[b], ph_done[b]);
+                for (int j = 0; j < 8; ++j) {
+                    const int co = 8 * part + j;
+                    v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] +
+                           bias[co < cout ? co : 0];
+                }
+                if constexpr (OUT_MODE == 0) {
+                    uint4* dst = reinterpret_cast<uint4*>(out);
+                    dst[blk_index<LOGD, 4>(x, yy, zz, part)] =
+                        make_uint4(pack_bf16x2(gelu_tc(v[0]), gelu_tc(v[1])), pack_bf16x2(gelu_tc(v[2]), gelu_tc(v[3])),
+                                   pack_bf16x2(gelu_tc(v[4]), gelu_tc(v[5])), pack_bf16x2(gelu_tc(v[6]), gelu_tc(v[7])));
+                } else if constexpr (OUT_MODE == 2 || OUT_MODE == 3) {
+                    const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
+                    float o[8];
+#pragma unroll
+                    for (int j = 0; j < 8; ++j) {
+                        const long long qi = (long long)(8 * part + j) * D3 + p;
+                        if constexpr (OUT_MODE == 2) {
+                            zbuf[qi] = v[j];
+                            o[j] = gelu_tc(v[j]);
+                        } else {
+                            o[j] = v[j] * gelu_grad_tc(zbuf[qi]);
+                        }
+                    }
+                    uint4* dst = reinterpret_cast<uint4*>(out);
+                    uint4* wg = reinterpret_cast<uint4*>(cm);
+                    const uint4 pk = make_uint4(pack_bf16x2(o[0], o[1]), pack_bf16x2(o[2], o[3]), pack_bf16x2(o[4], o[5]),
+                                                pack_bf16x2(o[6], o[7]));
+                    dst[blk_index<LOGD, 4>(x, yy, zz, part)] = pk;
+                    if constexpr (OUT_MODE == 2)
+                        wg[wga_index<LOGD, 32>(x, yy, part, zz)] = pk;
+                    else
+                        wgb_store<LOGD, 32>(wg, x, yy, part, zz, pk);
+                } else {
+                    float* dst = reinterpret_cast<float*>(out);
+                    const long long p = ((((long long)x << LOGD) + yy) << LOGD) | zz;
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (8 * part + j < cout) dst[(8 * part + j) * D3 + p] = v[j] * out_scale;
+                }
+            }
         }
     }
     tc_fence_before();
@@ -334,7 +361,6 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
     tc_fence_after();
     if (warp == 0) tmem_dealloc(tmem, kTcTmemCols);
 }
-
 
 // ------------------------------------------------------------------ training
 // Tensor-core training of the network (BF16 operands, FP32 accumulation,
