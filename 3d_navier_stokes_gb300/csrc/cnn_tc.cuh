@@ -253,6 +253,8 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
                 mma_commit(&done[b]);
                 pend_mma |= 1u << b;
                 // those MMAs read A buffer b: refill it with tile i + 2 once they are done
+                // (refilling the other buffer with tile i + 1 right after issuing these
+                // instead measured slower: its copies then land too late)
                 if (i + 2 < nmine) {
                     ok = mbar_wait(&done[b], (ph_done >> b) & 1u);
                     if (!ok) break;
@@ -273,6 +275,9 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
         const int quarter = warp & 3, part = warp >> 2;   // lane quarter, 8-channel group
         const int m = quarter * 32 + lane;
         const bool active = (NO == 32) || part < 2;
+        float bv[8];   // this thread's 8 biases, once
+#pragma unroll
+        for (int j = 0; j < 8; ++j) bv[j] = bias[8 * part + j < cout ? 8 * part + j : 0];
         uint32_t ph_done = 0u;
 #pragma unroll 1
         for (int i = 0; i < nmine; ++i) {
@@ -316,8 +321,7 @@ k_conv3_tc(const uint4* __restrict__ in, const uint4* __restrict__ wpk, const fl
 #pragma unroll
                 for (int j = 0; j < 8; ++j) {
                     const int co = 8 * part + j;
-                    v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] +
-                           bias[co < cout ? co : 0];
+                    v[j] = sX[co * 128 + left] + __uint_as_float(g0[j]) + sX[(NO + co) * 128 + right] + bv[j];
                 }
                 if constexpr (OUT_MODE == 0) {
                     uint4* dst = reinterpret_cast<uint4*>(out);
