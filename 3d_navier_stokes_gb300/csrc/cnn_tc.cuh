@@ -504,7 +504,13 @@ struct WgGeo {
     static constexpr uint32_t TAP_BYTES = (uint32_t)CI * D * 2;       // one wg-A line
     static constexpr uint32_t A_BYTES = 128u * D * 2;                 // one tap group
     static constexpr uint32_t B_BYTES = 3u * NB * D * 2;              // one wg-B line
-    static constexpr uint32_t STAGE = NGRP * A_BYTES + B_BYTES;
+    // the last group holds its taps and the ones slot; the rows of its unused slots are
+    // read from whatever follows (the B line, discarded rows), as long as the stage holds
+    // the group's full 128 rows
+    static constexpr uint32_t LAST_SLOTS = 9 - (NGRP - 1) * TG + 1;
+    static constexpr uint32_t A_REGION = (NGRP - 1) * A_BYTES + LAST_SLOTS * TAP_BYTES;
+    static constexpr uint32_t STAGE =
+        A_REGION + B_BYTES > NGRP * A_BYTES ? A_REGION + B_BYTES : NGRP * A_BYTES;
     static constexpr int NST = 225280u / STAGE >= 4 ? 4 : (225280u / STAGE >= 3 ? 3 : 2);
     static constexpr int ONES = (9 - (NGRP - 1) * TG) * CI;          // first padding row of the last group
     static constexpr int TCOLS = tc_pow2(NGRP * NN);
@@ -514,6 +520,7 @@ struct WgGeo {
     static constexpr uint32_t SMEM = need > floor_bytes ? need : floor_bytes;
     static constexpr int PART = NGRP * 128 * NN;   // floats of one CTA's partial sums
     static_assert(CI % 8 == 0 && NB % 16 == 0 && NGRP * TG > 9, "tile shape");
+    static_assert(LAST_SLOTS <= (uint32_t)TG && A_REGION % 16 == 0, "last tap group");
     static_assert(STAGE % 16 == 0 && TAP_BYTES % 16 == 0 && B_BYTES % 16 == 0, "bulk copy sizes");
     static_assert(NST * STAGE + 2 * NST * 8 + 16 <= 232448u, "shared memory");
 };
@@ -573,7 +580,7 @@ k_wgrad_tc(const uint4* __restrict__ a, const uint4* __restrict__ d, float* __re
                 bulk_g2s(sa + (t9 / TG) * WG::A_BYTES + (t9 % TG) * WG::TAP_BYTES,
                          a + ((((long long)gx << LOGD) + gy) * (CI / 8)) * D, WG::TAP_BYTES, &full[st]);
             }
-            bulk_g2s(sa + NGRP * WG::A_BYTES, d + (((long long)x << LOGD) + y) * 3 * (NB / 8) * D, WG::B_BYTES,
+            bulk_g2s(sa + WG::A_REGION, d + (((long long)x << LOGD) + y) * 3 * (NB / 8) * D, WG::B_BYTES,
                      &full[st]);
             pend_full |= 1u << st;
         };
@@ -587,7 +594,7 @@ k_wgrad_tc(const uint4* __restrict__ a, const uint4* __restrict__ d, float* __re
             ph_full ^= 1u << st;
             pend_full &= ~(1u << st);
             tc_fence_after();
-            const uint32_t a0 = s_u + st * WG::STAGE, b0 = a0 + NGRP * WG::A_BYTES;
+            const uint32_t a0 = s_u + st * WG::STAGE, b0 = a0 + WG::A_REGION;
 #pragma unroll 1
             for (int g = 0; g < NGRP; ++g)
 #pragma unroll 1
