@@ -41,7 +41,7 @@ EXPORTS = (
     "ns3d_ensemble_create", "ns3d_ensemble_destroy", "ns3d_ensemble_last_error",
     "ns3d_ensemble_initial_condition", "ns3d_ensemble_set_state_host", "ns3d_ensemble_get_state_host",
     "ns3d_ensemble_measurables", "ns3d_ensemble_get_time", "ns3d_ensemble_step", "ns3d_ensemble_info",
-    "ns3d_ensemble_run",
+    "ns3d_ensemble_run", "ns3d_ensemble_profile",
     "ns3d_ensemble_last_step_ms", "ns3d_set_state_real_host",
     "ns3d_les_num_params", "ns3d_les_create", "ns3d_les_destroy", "ns3d_les_last_error", "ns3d_les_add_snapshot",
     "ns3d_les_dataset_size", "ns3d_les_filtered_velocity_host", "ns3d_les_set_scales", "ns3d_les_get_scales",
@@ -216,6 +216,9 @@ def lib():
         L.ns3d_ensemble_run.argtypes = [P, I]
         L.ns3d_ensemble_info.restype = I
         L.ns3d_ensemble_info.argtypes = [P, ctypes.POINTER(I), ctypes.POINTER(I)]
+        L.ns3d_ensemble_profile.restype = I
+        L.ns3d_ensemble_profile.argtypes = [P, I, I, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(ctypes.c_float),
+                                            ctypes.POINTER(ctypes.c_double), I, ctypes.POINTER(I), ctypes.POINTER(I)]
         L.ns3d_ensemble_last_step_ms.restype = I
         L.ns3d_ensemble_last_step_ms.argtypes = [P, ctypes.POINTER(ctypes.c_float)]
         F = ctypes.POINTER(ctypes.c_float)
@@ -606,6 +609,17 @@ class Ensemble:
         v = ctypes.c_float()
         self._ck(lib().ns3d_ensemble_last_step_ms(self._h, ctypes.byref(v)))
         return v.value
+
+    def profile_group(self, group: int, reps: int = 3):
+        """(N, [(kernel class, ms per launch, bytes)]) of launch group `group`;
+        its members advance `reps` steps."""
+        names = (ctypes.c_char_p * 16)()
+        ms = (ctypes.c_float * 16)()
+        by = (ctypes.c_double * 16)()
+        cnt, n = ctypes.c_int(), ctypes.c_int()
+        self._ck(lib().ns3d_ensemble_profile(self._h, group, reps, names, ms, by, 16, ctypes.byref(cnt),
+                                             ctypes.byref(n)))
+        return n.value, [(names[i].decode(), ms[i], by[i]) for i in range(cnt.value)]
 
 
 

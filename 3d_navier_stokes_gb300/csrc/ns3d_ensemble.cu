@@ -329,4 +329,14 @@ ns3d_status ns3d_ensemble_last_step_ms(ns3d_ensemble* e, float* ms) {
     return cudaEventElapsedTime(ms, e->ev0, e->ev1) == cudaSuccess ? NS3D_OK : NS3D_ERR_CUDA;
 }
 
+ns3d_status ns3d_ensemble_profile(ns3d_ensemble* e, int group, int reps, const char** names, float* ms,
+                                  double* bytes, int max_count, int* count, int* n_out) {
+    if (!e || group < 0 || group >= (int)e->groups.size() || reps <= 0 || !names || !ms || !count)
+        return NS3D_ERR_INVALID;
+    if (n_out) *n_out = e->group_n[group];
+    const ns3d_status st = e->groups[group]->profile(reps, names, ms, bytes, max_count, count);
+    if (st != NS3D_OK) snprintf(e->err, sizeof(e->err), "%s", e->groups[group]->err());
+    return st;
+}
+
 }  // extern "C"

@@ -421,6 +421,11 @@ def run_ensemble(args, local):
     groups, kps = ens.info()
     pts = sum(n ** 3 for n in sizes)
     e0 = [ens.measurables(i)[0]["energy"] for i in (0, 32, 64, 88)]
+    # per launch group, after the timed steps: each kernel class's device time (ms per launch)
+    group_profile = {}
+    for g in range(groups):
+        n, prof = ens.profile_group(g, reps=3)
+        group_profile[str(n)] = {name: round(t, 4) for name, t, _ in prof}
     line = {"metric": "ensemble grid-pt*RK4-steps/s (96 runs: 32x48^3, 32x64^3, 24x96^3, 8x128^3)",
             "value": pts * args.steps / (ms / 1e3), "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -431,6 +436,7 @@ def run_ensemble(args, local):
             "timing": f"ns3d_ensemble_run: {args.steps} steps in one graph launch (a device-side while loop); "
                       f"one launch per step: {ms_per_launch / args.steps:.4f} ms/step",
             "autotune": {"seconds": tune_s, "choices": tuned},
+            "group_profile_ms": group_profile,
             "energy_samples": e0}
     print(json.dumps(line), flush=True)
     ens.close()

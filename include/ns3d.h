@@ -215,6 +215,12 @@ ns3d_status ns3d_ensemble_run(ns3d_ensemble* e, int nsteps);
 ns3d_status ns3d_ensemble_info(ns3d_ensemble* e, int* groups, int* kernels_per_step);
 /* device time of the last ns3d_ensemble_step / ns3d_ensemble_run call, milliseconds */
 ns3d_status ns3d_ensemble_last_step_ms(ns3d_ensemble* e, float* ms);
+/* ns3d_profile_step for launch group `group` (0 <= group < groups of
+ * ns3d_ensemble_info): device time of each kernel class of one step of all the
+ * group's members, over `reps` steps that advance those members; grid size N of
+ * the group in *n_out. */
+ns3d_status ns3d_ensemble_profile(ns3d_ensemble* e, int group, int reps, const char** names, float* ms,
+                                  double* bytes, int max_count, int* count, int* n_out);
 
 /* r2c + 2/3 dealiasing of a host velocity in the reference real layout
  * [N][N][N+2][3] into the state (InitialConditions' transform path,

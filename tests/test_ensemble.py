@@ -64,3 +64,26 @@ def test_ensemble_run_is_one_launch_of_the_same_steps(ns3d):
         assert a.get_time(i) == b.get_time(i)
     a.close()
     b.close()
+
+
+def test_group_profile(ns3d):
+    """ns3d_ensemble_profile: per launch group, the device time of each kernel
+    class of one step of all the group's members."""
+    members = [dict(N=32, nu=0.01, dt=1e-3, precision="fp32") for _ in range(3)] + \
+              [dict(N=48, nu=0.01, dt=1e-3, precision="fp32") for _ in range(2)]
+    ens = ns3d.Ensemble(members)
+    for m in range(len(members)):
+        ens.InitialConditions(m, "SPECTRUM", seed=m, k0=3.0)
+    groups, _ = ens.info()
+    assert groups == 2
+    seen = set()
+    for g in range(groups):
+        n, prof = ens.profile_group(g, reps=2)
+        seen.add(n)
+        names = [p[0] for p in prof]
+        assert "k_xinv" in names and "k_xfwd" in names and len(prof) == 6
+        assert all(t >= 0.0 for _, t, _ in prof) and sum(t for _, t, _ in prof) > 0.0
+    assert seen == {32, 48}
+    with pytest.raises(ns3d.NS3DError):
+        ens.profile_group(groups)
+    ens.close()
