@@ -51,6 +51,20 @@ def workload(N: int) -> dict:
                 l2=f"inputs larger than L2: each state field {field_mb:.0f} MB > 129 MB L2")
 
 
+def lr_chunks(iters: int, schedule: str):
+    """The Adam training of the LES mode as (iterations, learning rate) chunks: "const" is lr 1e-3
+    throughout; "step" is 1e-3, 3e-4 and 1e-4 over 50 / 30 / 20 % of the iterations (the last chunk
+    takes the remainder, so the chunks add up to iters)."""
+    sched = [(1.0, 1e-3)] if schedule == "const" else [(0.5, 1e-3), (0.3, 3e-4), (0.2, 1e-4)]
+    out, done = [], 0
+    for i, (frac, lr) in enumerate(sched):
+        it = iters - done if i == len(sched) - 1 else int(round(frac * iters))
+        if it > 0:
+            out.append((it, lr))
+        done += it
+    return out
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -459,7 +473,6 @@ def run_les(args, local):
     dns.InitialConditions("SPECTRUM", seed=0, k0=3.0)
     dns.RK4Step(500)
     nseed = max(1, args.les_seeds)
-    sched = [(1.0, 1e-3)] if args.lr_schedule == "const" else [(0.5, 1e-3), (0.3, 3e-4), (0.2, 1e-4)]
     nets = [pkg.LES(Nc, capacity=args.snapshots, seed=s) for s in range(nseed)]
     t0 = time.perf_counter()
     for _ in range(args.snapshots):
@@ -471,12 +484,9 @@ def run_les(args, local):
     t_train, loss_tr, loss1 = [], [], []
     for les in nets:
         t0 = time.perf_counter()
-        done = 0
-        for i, (frac, lr) in enumerate(sched):
-            it = args.train_iters - done if i == len(sched) - 1 else int(round(frac * args.train_iters))
-            if it > 0:
-                tail = les.train(it, lr=lr)
-            done += it
+        tail = 0.0
+        for it, lr in lr_chunks(args.train_iters, args.lr_schedule):
+            tail = les.train(it, lr=lr)
         t_train.append(time.perf_counter() - t0)
         loss_tr.append(tail)
         loss1.append(les.dataset_loss())
