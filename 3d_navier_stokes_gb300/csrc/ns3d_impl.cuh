@@ -78,7 +78,7 @@ class Impl final : public Base {
         for (void* q : {(void*)U_, (void*)UT_, (void*)ACC_, (void*)W_, (void*)tw_, (void*)tab_, (void*)part_,
                         (void*)mout_, (void*)stage_, (void*)real_, (void*)sd_, (void*)TAU_, (void*)F_,
                         (void*)tau_real_, (void*)sgs_part_, (void*)K_, (void*)dpart_, (void*)plan_out_.ranges, (void*)plan_in_.ranges,
-                        (void*)zg_b_, (void*)zg_P_})
+                        (void*)zg_b_, (void*)zg_P_, (void*)xt_items_})
             if (q) cudaFree(q);
         if (sd_host_) cudaFreeHost(sd_host_);
         if (mout_host_) cudaFreeHost(mout_host_);
@@ -181,6 +181,8 @@ class Impl final : public Base {
             NS3D_CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_xinv_tma<T, N, V>,
                                                                   xtma_tile<T, N, V>() * PX::P, xinv_tma_smem<T, N, V>()));
             xt_ctas_ = (per_sm > 0 ? per_sm : 1) * nsm;
+            ns3d_status st = build_xitems(xtma_tile<T, N, V>(), &xt_items_, &xt_nvalid_);
+            if (st != NS3D_OK) return st;
         }
         set_xfwd_attrs<INT_IFRK4>();
         set_xfwd_attrs<INT_RK4CN>();
@@ -201,6 +203,20 @@ class Impl final : public Base {
         return sizeof(cx<T>) * (size_t)ZP * 3 * zpad<N>() + sizeof(T) * (size_t)ZP * 12 * N;
     }
 
+    // the compact list of the x tiles of TT pencils whose first column lies inside the
+    // circle ky^2 + kz0^2 <= KC^2, ky-major: entry ((ky + KC) << 8) | tile
+    ns3d_status build_xitems(int TT, int** dev, int* count) {
+        std::vector<int> v;
+        const int ntx = (G::NZ1 + TT - 1) / TT;
+        for (int ky = -G::KC; ky <= G::KC; ++ky)
+            for (int tl = 0; tl < ntx; ++tl)
+                if (ky * ky + tl * TT * tl * TT <= G::KC2) v.push_back(((ky + G::KC) << 8) | tl);
+        NS3D_CK(cudaMalloc(dev, sizeof(int) * v.size()));
+        NS3D_CK(cudaMemcpy(*dev, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
+        *count = (int)v.size();
+        return NS3D_OK;
+    }
+
     template <int INTEG>
     void set_xfwd_attrs() {
         cudaFuncSetAttribute(k_xfwd<T, N, INTEG, X_STAGE1, V>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_x());
@@ -217,10 +233,10 @@ class Impl final : public Base {
             const int k = in == U_ ? 0 : (in == UT_ ? 1 : -1);
             if (k >= 0) {
                 constexpr int XT = xtma_tile<T, N, V>();
-                const long long items = (long long)((G::NZ1 + XT - 1) / XT) * G::NKY * cnt;
+                const long long items = (long long)xt_nvalid_ * cnt;
                 const unsigned grid = (unsigned)(items < xt_ctas_ ? items : xt_ctas_);
-                k_xinv_tma<T, N, V><<<grid, XT * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(xmap_[k], 3 * m0, Wm(m0), tw_,
-                                                                                       sdm(m0), cnt);
+                k_xinv_tma<T, N, V><<<grid, XT * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(
+                    xmap_[k], 3 * m0, Wm(m0), tw_, sdm(m0), xt_items_, xt_nvalid_, cnt);
                 return;
             }
         }
@@ -1075,6 +1091,8 @@ class Impl final : public Base {
     int zg_ctas_ = 0;
     CUtensorMap xmap_[2];          // P1 tensor-tile form: U and UT as [3 M][N kx][N ky][2 NZP] FP32
     int xt_ctas_ = 1;
+    int* xt_items_ = nullptr;      // P1 tensor-tile form: compact list of the x tiles inside the circle
+    int xt_nvalid_ = 0;
     double* sgs_part_ = nullptr;
     cx<T>* K_ = nullptr;           // RK5 family: stored stages [member][6][3]
     double* dpart_ = nullptr;      // DP5CN error partial sums [member][block][3]

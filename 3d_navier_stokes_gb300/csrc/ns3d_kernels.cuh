@@ -375,7 +375,8 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 }
 // ---------------------------------------------------------------------------
 // P1, tensor-tile form (FP32, the x plans of variant 3). Persistent CTAs walk
-// the (member, ky, kz-tile) items inside the circle ky^2 + kz^2 <= KC^2. Thread
+// the (member, ky, kz-tile) items inside the circle ky^2 + kz^2 <= KC^2 (a
+// compact list, so that every CTA gets the same number of items). Thread
 // 0 copies each velocity component of a tile into one of two slabs [kx][TT]
 // with cp.async.bulk.tensor boxes of XB kx rows x TT pencils, only the rows
 // |kx| <= kxmax of the tile's widest column (the rest of a slab is stale and
@@ -388,6 +389,19 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // on a timeout the CTA records kStatusTimeout, waits for its own copies and
 // returns.
 // ---------------------------------------------------------------------------
+// The compact list of the (ky, kz-tile) items whose first column lies inside
+// the circle ky^2 + kz0^2 <= KC^2, built on the host in ky-major order: entry
+// ((ky + KC) << 8) | tile. Item `it` of member m is entry it - m * nvalid; CTAs
+// take items it = blockIdx.x + k gridDim.x, so every CTA gets the same number
+// of items to within one (skipping the items outside the circle in a full
+// (ky, tile) grid instead left 18 to 22 items per CTA at 512^3).
+__device__ __forceinline__ void xtile_item(const int* __restrict__ xitems, int nvalid, int it, int kc, int tt,
+                                           int& m, int& ky, int& kz0) {
+    m = it / nvalid;
+    const int e = __ldg(&xitems[it - m * nvalid]);
+    ky = (e >> 8) - kc;
+    kz0 = (e & 255) * tt;
+}
 template <int N> constexpr int xbox_rows() { return N % 32 == 0 ? 32 : 16; }
 // pencils per CTA and CTAs per SM: variant 3's x tiles, one CTA per SM (8-pencil
 // tiles at two CTAs per SM spill 330 bytes per thread at 512^3 under the 128-register cap)
@@ -405,39 +419,29 @@ constexpr bool xinv_tma_ok() {
 template <typename T, int N, int V>
 __global__ void __launch_bounds__(xtma_tile<T, N, V>() * PlansV<N, V>::X::P, xtma_minb<T, N, V>())
 k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw,
-           StepDev* __restrict__ sd, int cnt) {
+           StepDev* __restrict__ sd, const int* __restrict__ xitems, int nvalid, int cnt) {
     using G = Geo<N>;
     using PL = typename PlansV<N, V>::X;
     constexpr int TT = xtma_tile<T, N, V>();
     constexpr int E = PL::E, P = PL::P;
     constexpr int XB = xbox_rows<N>();
     constexpr uint32_t BOX_BYTES = (uint32_t)XB * TT * sizeof(cx<T>);
-    constexpr int NTX = (G::NZ1 + TT - 1) / TT;
-    constexpr long long PER_MEM = (long long)NTX * G::NKY;
     extern __shared__ __align__(128) unsigned char smem_raw[];
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);       // exchange [N][TT]
     cx<T>* slab0 = sbuf + (size_t)N * TT;                    // [2][N][TT]
     uint64_t* bars = reinterpret_cast<uint64_t*>(slab0 + 2 * (size_t)N * TT);
     const int tid = threadIdx.x;
     const int t = tid % TT, p = tid / TT;
-    const long long items = PER_MEM * cnt;
+    const int items = nvalid * cnt;
     const T scale = T(1) / (T(N) * T(N) * T(N));
     const long long budget = sd[0].wait_cycles > 0 ? sd[0].wait_cycles : kWaitCycles;
     StridedIdx<TT, PL::R1> sidx{t};
     SyncBlock sync;
 
-    auto next_valid = [&](long long it) {
-        for (; it < items; it += gridDim.x) {
-            const int r = (int)(it % PER_MEM);
-            const int ky = r / NTX - G::KC, kz0 = (r % NTX) * TT;
-            if (ky * ky + kz0 * kz0 <= G::KC2) break;
-        }
-        return it;
-    };
     // thread 0: component c of item `it` into slab sl
-    auto issue = [&](long long it, int c, int sl) {
-        const int m = (int)(it / PER_MEM), r = (int)(it % PER_MEM);
-        const int ky = r / NTX - G::KC, kz0 = (r % NTX) * TT;
+    auto issue = [&](int it, int c, int sl) {
+        int m, ky, kz0;
+        xtile_item(xitems, nvalid, it, G::KC, TT, m, ky, kz0);
         const int j = ky < 0 ? ky + N : ky;
         const int r2 = G::KC2 - ky * ky - kz0 * kz0;
         int kxm = (int)sqrtf((float)r2);
@@ -466,7 +470,7 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
         fence_barrier_init();
     }
     __syncthreads();
-    long long it = next_valid(blockIdx.x);
+    int it = blockIdx.x;
     int sx = 0, sy = 1;       // slabs holding this item's ux and uy
     uint32_t ph = 0u;         // bit sl: parity of the next completion of slab sl
     uint32_t pend = 0u;       // thread 0: slabs with a copy in flight
@@ -493,15 +497,16 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
     };
 
     while (it < items) {
-        const int m = (int)(it / PER_MEM), r = (int)(it % PER_MEM);
-        const int ky = r / NTX - G::KC, kz = (r % NTX) * TT + t;
+        int m, ky, kz0;
+        xtile_item(xitems, nvalid, it, G::KC, TT, m, ky, kz0);
+        const int kz = kz0 + t;
         const int j = ky < 0 ? ky + N : ky;
         const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
         const int rem = G::KC2 - ky * ky - kz * kz;
         const long long off = (long long)j * G::NZP + kz;
         const long long xs = (long long)N * G::NZP;
         cx<T>* Wm = W + (long long)m * 6 * G::FS;
-        const long long nx = next_valid(it + gridDim.x);
+        const int nx = it + (int)gridDim.x;
         auto read = [&](int sl, cx<T>(&v)[E]) {
             const cx<T>* src = slab0 + (size_t)sl * N * TT + t;
 #pragma unroll
@@ -1066,6 +1071,142 @@ k_zline(cx<T>* __restrict__ W, const cx<T>* __restrict__ tw, StepDev* __restrict
     }
     flush_umax();
 }
+// The stage epilogue reads the state of each of its modes after the FFT. Its
+// rows (TT modes of one x row, per array and component: one 16-byte aligned
+// segment each) are prefetched into L2 before the FFT, spread over the TT
+// threads of a row, so that those loads hit L2. Tile (ky, kz0 .. kz0 + TT).
+template <typename T, int N, int INTEG, int MODE, int E, int P, int TT>
+__device__ __forceinline__ void xfwd_prefetch_state(const cx<T>* U, const cx<T>* ACC, const cx<T>* K,
+                                                    const RkStage& rs, int p, int t, int ky, int kz0, int j) {
+    if constexpr (MODE <= X_STAGE4) {
+        using G = Geo<N>;
+        const long long xs = (long long)N * G::NZP;
+        const int rem0 = G::KC2 - ky * ky - kz0 * kz0;
+        const uint32_t seg = (uint32_t)((TT < G::NZP - kz0 ? TT : G::NZP - kz0) * sizeof(cx<T>));
+        constexpr bool kIF = INTEG == INT_IFRK4;
+        constexpr bool needU = !(kIF && MODE == X_STAGE4);
+        constexpr bool needA = INTEG != INT_TAB && MODE != X_STAGE1;
+        for (int s = t; s < E; s += TT) {
+            const int kx = kof<N>(p + P * s);
+            if (kx * kx > rem0) continue;
+            const long long q = (long long)(p + P * s) * xs + (long long)j * G::NZP + kz0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                if (needU) bulk_prefetch_l2(U + c * G::FS + q, seg);
+                if (needA) bulk_prefetch_l2(ACC + c * G::FS + q, seg);
+                if constexpr (INTEG == INT_TAB) {
+                    for (int jj = 0; jj < rs.nk && jj < 6; ++jj)
+                        if (rs.c[jj] != 0.0 || rs.e[jj] != 0.0)
+                            bulk_prefetch_l2(K + (long long)jj * 3 * G::FS + c * G::FS + q, seg);
+                }
+            }
+        }
+    }
+}
+// RK4-family stage epilogue (IF-RK4, RK4CN) of one thread's E modes, the x rows
+// p + P s of the column (ky, kz) inside the sphere: the Leray projection of every
+// mode first, then, in chunks of up to 8 modes and per component, the chunk's
+// state loads before their updates, so that a chunk's loads (per array) are in
+// flight at once.
+template <typename T, int N, int INTEG, int MODE, int E, int P>
+__device__ __forceinline__ void xfwd_rk4_epilogue(cx<T> (&F)[3][E], int p, int ky, int kz, long long off,
+                                                  cx<T>* __restrict__ U, cx<T>* __restrict__ UT,
+                                                  cx<T>* __restrict__ ACC, const cx<T>* __restrict__ tab,
+                                                  const StepDev* __restrict__ sd, const cx<T>* __restrict__ sgs, T h) {
+    using G = Geo<N>;
+    const long long xs = (long long)N * G::NZP;
+    const int rem = G::KC2 - ky * ky - kz * kz;
+    constexpr int CH = E > 8 ? 4 : E;
+    unsigned valid = 0u;
+    int k2s[E];
+#pragma unroll
+    for (int s = 0; s < E; ++s) {
+        const int i = p + P * s;
+        const int kx = kof<N>(i);
+        k2s[s] = 0;
+        if (kx * kx > rem) continue;
+        valid |= 1u << s;
+        const int k2 = kx * kx + ky * ky + kz * kz;
+        cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
+        if (sgs && sd->sgs_on) {
+            // learned subgrid term -div(tau), single run only (member 0)
+            const long long q = (long long)i * xs + off;
+            n0 = n0 + sgs[q];
+            n1 = n1 + sgs[G::FS + q];
+            n2 = n2 + sgs[2 * G::FS + q];
+        }
+        if (k2 > 0) {
+            const T kinv = T(1) / T(k2);
+            const cx<T> kdn = n0 * T(kx) + n1 * T(ky) + n2 * T(kz);
+            n0 = n0 - kdn * (T(kx) * kinv);
+            n1 = n1 - kdn * (T(ky) * kinv);
+            n2 = n2 - kdn * (T(kz) * kinv);
+        } else {
+            n0 = n1 = n2 = czero<T>();
+        }
+        F[0][s] = n0;
+        F[1][s] = n1;
+        F[2][s] = n2;
+        k2s[s] = k2;
+    }
+    constexpr bool kIF = INTEG == INT_IFRK4;
+    constexpr bool needU = !(kIF && MODE == X_STAGE4);
+    constexpr bool needA = kIF ? (MODE != X_STAGE1) : (MODE != X_STAGE1);
+#pragma unroll
+    for (int s0 = 0; s0 < E; s0 += CH) {
+      if (!((valid >> s0) & ((1u << CH) - 1u))) continue;
+      cx<T> tb[CH];
+#pragma unroll
+      for (int s = 0; s < CH; ++s) tb[s] = ldg(&tab[k2s[s0 + s]]);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        cx<T> u[CH], a[CH];
+#pragma unroll
+        for (int s = 0; s < CH; ++s) {
+            u[s] = czero<T>();
+            a[s] = czero<T>();
+            if (!((valid >> (s0 + s)) & 1u)) continue;
+            const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
+            if (needU) u[s] = U[q];
+            if (needA) a[s] = ACC[q];
+        }
+#pragma unroll
+        for (int s = 0; s < CH; ++s) {
+            if (!((valid >> (s0 + s)) & 1u)) continue;
+            const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
+            const cx<T> nn = F[c][s0 + s];
+            if constexpr (kIF) {
+                const T Eh = tb[s].x, Ef = tb[s].y;
+                if (MODE == X_STAGE1) {
+                    UT[q] = (u[s] + nn * (h * T(0.5))) * Eh;
+                    ACC[q] = (u[s] + nn * (h / T(6))) * Ef;
+                } else if (MODE == X_STAGE2) {
+                    UT[q] = u[s] * Eh + nn * (h * T(0.5));
+                    ACC[q] = a[s] + nn * (h / T(3) * Eh);
+                } else if (MODE == X_STAGE3) {
+                    UT[q] = u[s] * Ef + nn * (h * Eh);
+                    ACC[q] = a[s] + nn * (h / T(3) * Eh);
+                } else {
+                    U[q] = a[s] + nn * (h / T(6));
+                }
+            } else {
+                if (MODE == X_STAGE1) {
+                    UT[q] = u[s] + nn * (h * T(0.5));
+                    ACC[q] = nn * (T(1) / T(6));
+                } else if (MODE == X_STAGE2) {
+                    UT[q] = u[s] + nn * (h * T(0.5));
+                    ACC[q] = a[s] + nn * (T(1) / T(3));
+                } else if (MODE == X_STAGE3) {
+                    UT[q] = u[s] + nn * h;
+                    ACC[q] = a[s] + nn * (T(1) / T(3));
+                } else {
+                    U[q] = u[s] * tb[s].x + (a[s] + nn * (T(1) / T(6))) * tb[s].y;
+                }
+            }
+        }
+      }
+    }
+}
 // ---------------------------------------------------------------------------
 // P5: forward FFT along x of the 3 product fields, then per mode the Leray
 // projection, dealias mask and RK stage update. grid (ntile, NKY).
@@ -1122,32 +1263,7 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
 #pragma unroll
         for (int s = 0; s < E; ++s) F[c][s] = colok ? src[(long long)(p + P * s) * xs] : czero<T>();
     }
-    if constexpr (MODE <= X_STAGE4) {
-        // The epilogue reads the state of each of its modes after the FFT. Its
-        // rows (TT modes of one x row, per array and component: one 16-byte
-        // aligned segment each) are prefetched into L2 now, spread over the
-        // TT threads of a row, so that those loads hit L2.
-        const int rem0 = G::KC2 - ky * ky - kz0 * kz0;
-        const uint32_t seg = (uint32_t)((TT < G::NZP - kz0 ? TT : G::NZP - kz0) * sizeof(cx<T>));
-        constexpr bool kIF = INTEG == INT_IFRK4;
-        constexpr bool needU = !(kIF && MODE == X_STAGE4);
-        constexpr bool needA = INTEG != INT_TAB && MODE != X_STAGE1;
-        for (int s = t; s < E; s += TT) {
-            const int kx = kof<N>(p + P * s);
-            if (kx * kx > rem0) continue;
-            const long long q = (long long)(p + P * s) * xs + (long long)j * G::NZP + kz0;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) {
-                if (needU) bulk_prefetch_l2(U + c * G::FS + q, seg);
-                if (needA) bulk_prefetch_l2(ACC + c * G::FS + q, seg);
-                if constexpr (INTEG == INT_TAB) {
-                    for (int jj = 0; jj < rs.nk && jj < 6; ++jj)
-                        if (rs.c[jj] != 0.0 || rs.e[jj] != 0.0)
-                            bulk_prefetch_l2(K + (long long)jj * 3 * G::FS + c * G::FS + q, seg);
-                }
-            }
-        }
-    }
+    xfwd_prefetch_state<T, N, INTEG, MODE, E, P, TT>(U, ACC, K, rs, p, t, ky, kz0, j);
 #pragma unroll
     for (int c = 0; c < 3; ++c) PL::fwd(F[c], sbuf, p, tw, sidx, sync);
     if (INTEG != INT_TAB && !colok) return;
@@ -1156,100 +1272,7 @@ k_xfwd(const cx<T>* __restrict__ W, cx<T>* __restrict__ U, cx<T>* __restrict__ U
     if (MODE <= X_STAGE4) h = T(sd->dt);
     const int rem = G::KC2 - ky * ky - kz * kz;
     if constexpr ((INTEG == INT_IFRK4 || INTEG == INT_RK4CN) && MODE <= X_STAGE4 && TileVar<V>::BATCH) {
-        // RK4-family stages: the projection of every mode of this thread first,
-        // then, in chunks of up to 8 modes and per component, the chunk's state
-        // loads before their updates, so that a chunk's loads (per array) are in
-        // flight at once
-        constexpr int CH = E > 8 ? 4 : E;
-        unsigned valid = 0u;
-        int k2s[E];
-#pragma unroll
-        for (int s = 0; s < E; ++s) {
-            const int i = p + P * s;
-            const int kx = kof<N>(i);
-            k2s[s] = 0;
-            if (kx * kx > rem) continue;
-            valid |= 1u << s;
-            const int k2 = kx * kx + ky * ky + kz * kz;
-            cx<T> n0 = F[0][s], n1 = F[1][s], n2 = F[2][s];
-            if (sgs && sd->sgs_on) {
-                // learned subgrid term -div(tau), single run only (member 0)
-                const long long q = (long long)i * xs + off;
-                n0 = n0 + sgs[q];
-                n1 = n1 + sgs[G::FS + q];
-                n2 = n2 + sgs[2 * G::FS + q];
-            }
-            if (k2 > 0) {
-                const T kinv = T(1) / T(k2);
-                const cx<T> kdn = n0 * T(kx) + n1 * T(ky) + n2 * T(kz);
-                n0 = n0 - kdn * (T(kx) * kinv);
-                n1 = n1 - kdn * (T(ky) * kinv);
-                n2 = n2 - kdn * (T(kz) * kinv);
-            } else {
-                n0 = n1 = n2 = czero<T>();
-            }
-            F[0][s] = n0;
-            F[1][s] = n1;
-            F[2][s] = n2;
-            k2s[s] = k2;
-        }
-        constexpr bool kIF = INTEG == INT_IFRK4;
-        constexpr bool needU = !(kIF && MODE == X_STAGE4);
-        constexpr bool needA = kIF ? (MODE != X_STAGE1) : (MODE != X_STAGE1);
-#pragma unroll
-        for (int s0 = 0; s0 < E; s0 += CH) {
-          if (!((valid >> s0) & ((1u << CH) - 1u))) continue;
-          cx<T> tb[CH];
-#pragma unroll
-          for (int s = 0; s < CH; ++s) tb[s] = ldg(&tab[k2s[s0 + s]]);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            cx<T> u[CH], a[CH];
-#pragma unroll
-            for (int s = 0; s < CH; ++s) {
-                u[s] = czero<T>();
-                a[s] = czero<T>();
-                if (!((valid >> (s0 + s)) & 1u)) continue;
-                const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
-                if (needU) u[s] = U[q];
-                if (needA) a[s] = ACC[q];
-            }
-#pragma unroll
-            for (int s = 0; s < CH; ++s) {
-                if (!((valid >> (s0 + s)) & 1u)) continue;
-                const long long q = c * G::FS + (long long)(p + P * (s0 + s)) * xs + off;
-                const cx<T> nn = F[c][s0 + s];
-                if constexpr (kIF) {
-                    const T Eh = tb[s].x, Ef = tb[s].y;
-                    if (MODE == X_STAGE1) {
-                        UT[q] = (u[s] + nn * (h * T(0.5))) * Eh;
-                        ACC[q] = (u[s] + nn * (h / T(6))) * Ef;
-                    } else if (MODE == X_STAGE2) {
-                        UT[q] = u[s] * Eh + nn * (h * T(0.5));
-                        ACC[q] = a[s] + nn * (h / T(3) * Eh);
-                    } else if (MODE == X_STAGE3) {
-                        UT[q] = u[s] * Ef + nn * (h * Eh);
-                        ACC[q] = a[s] + nn * (h / T(3) * Eh);
-                    } else {
-                        U[q] = a[s] + nn * (h / T(6));
-                    }
-                } else {
-                    if (MODE == X_STAGE1) {
-                        UT[q] = u[s] + nn * (h * T(0.5));
-                        ACC[q] = nn * (T(1) / T(6));
-                    } else if (MODE == X_STAGE2) {
-                        UT[q] = u[s] + nn * (h * T(0.5));
-                        ACC[q] = a[s] + nn * (T(1) / T(3));
-                    } else if (MODE == X_STAGE3) {
-                        UT[q] = u[s] + nn * h;
-                        ACC[q] = a[s] + nn * (T(1) / T(3));
-                    } else {
-                        U[q] = u[s] * tb[s].x + (a[s] + nn * (T(1) / T(6))) * tb[s].y;
-                    }
-                }
-            }
-          }
-        }
+        xfwd_rk4_epilogue<T, N, INTEG, MODE, E, P>(F, p, ky, kz, off, U, UT, ACC, tab, sd, sgs, h);
         return;
     }
     double es[3] = {0.0, 0.0, 0.0};   // DP5CN error partial sums

@@ -65,6 +65,32 @@ def lr_chunks(iters: int, schedule: str):
     return out
 
 
+def host_link(h2d: int, d2h: int, stream, e2e_step_ms: float, step_ms: float, reps: int = 3):
+    """The host link's copy rates for the e2e leg's byte counts: one pinned -> device and one
+    device -> pinned copy of the same sizes (DMA, CUDA events on the solver stream). The
+    transfer floor is the time those bytes take at those rates; the e2e step cannot go below
+    that floor plus the device step while the transfers and the step run one after the other."""
+    import torch
+    hb = torch.empty(max(h2d, d2h), dtype=torch.uint8, pin_memory=True)
+    db = torch.empty(max(h2d, d2h), dtype=torch.uint8, device="cuda")
+    rates = {}
+    with torch.cuda.stream(stream):
+        for name, nb, dst, src in (("h2d", h2d, db, hb), ("d2h", d2h, hb, db)):
+            dst[:nb].copy_(src[:nb], non_blocking=True)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for _ in range(reps):
+                dst[:nb].copy_(src[:nb], non_blocking=True)
+            e1.record(stream)
+            e1.synchronize()
+            rates[name] = reps * nb / (e0.elapsed_time(e1) / 1e3) / 1e9
+    floor = h2d / rates["h2d"] / 1e6 + d2h / rates["d2h"] / 1e6
+    del hb, db
+    return {"h2d_GBps": rates["h2d"], "d2h_GBps": rates["d2h"], "transfer_floor_ms": floor,
+            "device_step_ms": step_ms, "e2e_step_ms": e2e_step_ms,
+            "frac_of_serial_bound": (floor + step_ms) / e2e_step_ms}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -359,7 +385,8 @@ def run_ours(args, ws, rank, local):
         e2e = {"value": ws * N ** 3 * ke / (e2e_ms / 1e3), "unit": UNIT, "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "host_array_bytes": nbytes, "steps": ke,
                "call": "ns3d_step_host(ctx, u_hat_in, u_hat_out), reference layout complex128[N][N][N/2+1][3], "
-                       "pinned host arrays"}
+                       "pinned host arrays",
+               "link": host_link(h2d, d2h, stream, e2e_ms / ke, ms_max / args.steps)}
     s.close()
 
     fp64 = None
