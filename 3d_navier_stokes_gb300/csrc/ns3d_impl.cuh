@@ -169,7 +169,11 @@ class Impl final : public Base {
             const uint64_t strides[3] = {sizeof(cx<T>) * (uint64_t)G::NZP, sizeof(cx<T>) * (uint64_t)N * G::NZP,
                                          sizeof(cx<T>) * (uint64_t)G::FS};
             const uint32_t box[4] = {2u * (uint32_t)xtma_tile<T, N, V>(), 1u, (uint32_t)xbox_rows<N>(), 1u};
-            if (!encode_map4_f32(&xmap_[0], U_, dims, strides, box) || !encode_map4_f32(&xmap_[1], UT_, dims, strides, box)) {
+            // and one over the 6 M fields of W for its bulk tensor stores
+            const uint64_t wdims[4] = {2ull * G::NZP, (uint64_t)N, (uint64_t)N, 6ull * (uint64_t)M_};
+            const uint32_t wbox[4] = {2u * (uint32_t)xtma_tile<T, N, V>(), 1u, (uint32_t)xout_rows<N>(), 1u};
+            if (!encode_map4_f32(&xmap_[0], U_, dims, strides, box) || !encode_map4_f32(&xmap_[1], UT_, dims, strides, box) ||
+                !encode_map4_f32(&wmap_, W_, wdims, strides, wbox)) {
                 set_err("cuTensorMapEncodeTiled failed for the x-inverse pass");
                 return NS3D_ERR_CUDA;
             }
@@ -236,7 +240,7 @@ class Impl final : public Base {
                 const long long items = (long long)xt_nvalid_ * cnt;
                 const unsigned grid = (unsigned)(items < xt_ctas_ ? items : xt_ctas_);
                 k_xinv_tma<T, N, V><<<grid, XT * PX::P, xinv_tma_smem<T, N, V>(), s_>>>(
-                    xmap_[k], 3 * m0, Wm(m0), tw_, sdm(m0), xt_items_, xt_nvalid_, cnt);
+                    xmap_[k], 3 * m0, wmap_, 6 * m0, tw_, sdm(m0), xt_items_, xt_nvalid_, cnt);
                 return;
             }
         }
@@ -1090,6 +1094,7 @@ class Impl final : public Base {
     float* zg_P_ = nullptr;        // z-pass form 2: the three real-space products [member][3][N^3]
     int zg_ctas_ = 0;
     CUtensorMap xmap_[2];          // P1 tensor-tile form: U and UT as [3 M][N kx][N ky][2 NZP] FP32
+    CUtensorMap wmap_;             // and W as [6 M][N x][N ky][2 NZP] FP32 (its outputs)
     int xt_ctas_ = 1;
     int* xt_items_ = nullptr;      // P1 tensor-tile form: compact list of the x tiles inside the circle
     int xt_nvalid_ = 0;

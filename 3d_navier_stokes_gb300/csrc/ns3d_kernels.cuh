@@ -384,10 +384,14 @@ k_xinv(const cx<T>* __restrict__ U, cx<T>* __restrict__ W, const cx<T>* __restri
 // Per item: ux and uy are read from their slabs, which then receive this item's
 // uz and the next item's ux; uz is read twice (for wy and for itself) and its
 // slab then receives the next item's uy. Every copy is issued at least two of
-// the item's five transforms before it is read. The transforms and their
-// arithmetic are those of k_xinv (results bit-identical). Waits are bounded;
-// on a timeout the CTA records kStatusTimeout, waits for its own copies and
-// returns.
+// the item's five transforms before it is read. A slab holds only the rows
+// that can lie inside the sphere (SR of N). The six output fields leave through
+// an output buffer [N][TT] and bulk tensor stores over a 4D map of W (whole
+// tiles: the columns outside the circle, which no later pass reads, receive
+// zeros), so no warp waits on a queue of per-thread stores. The transforms and
+// their arithmetic are those of k_xinv (results bit-identical). Waits are
+// bounded; on a timeout the CTA records kStatusTimeout, waits for its own
+// copies and returns.
 // ---------------------------------------------------------------------------
 // The compact list of the (ky, kz-tile) items whose first column lies inside
 // the circle ky^2 + kz0^2 <= KC^2, built on the host in ky-major order: entry
@@ -407,19 +411,31 @@ template <int N> constexpr int xbox_rows() { return N % 32 == 0 ? 32 : 16; }
 // tiles at two CTAs per SM spill 330 bytes per thread at 512^3 under the 128-register cap)
 template <typename T, int N, int V> constexpr int xtma_tile() { return tile_x<T, N, V>(); }
 template <typename T, int N, int V> constexpr int xtma_minb() { return 1; }
+// rows of an input slab: the XB-row boxes that can hold |kx| <= KC from both ends of
+// the kx axis (all N rows when those meet)
+template <int N> constexpr int xtma_slab_rows() {
+    return 2 * (Geo<N>::KC / xbox_rows<N>() + 1) * xbox_rows<N>() < N
+               ? 2 * (Geo<N>::KC / xbox_rows<N>() + 1) * xbox_rows<N>()
+               : N;
+}
+// x rows per output box (bulk tensor store)
+template <int N> constexpr int xout_rows() { return N <= 256 ? N : N / 2; }
+// exchange buffer and output buffer [N][TT], two input slabs [SR][TT], two mbarriers
 template <typename T, int N, int V>
-constexpr size_t xinv_tma_smem() { return sizeof(cx<T>) * (size_t)N * xtma_tile<T, N, V>() * 3 + 16; }
+constexpr size_t xinv_tma_smem() {
+    return sizeof(cx<T>) * (size_t)xtma_tile<T, N, V>() * (2 * (size_t)N + 2 * (size_t)xtma_slab_rows<N>()) + 16;
+}
 template <typename T, int N, int V>
 constexpr bool xinv_tma_ok() {
     // not at 1024^3 (8-pencil tiles, 64-byte boxes): 5.17 ms per pass against 4.30 ms for k_xinv
     return sizeof(T) == 4 && V == 3 && N % 16 == 0 && N >= 48 && N <= 512 && xinv_tma_smem<T, N, V>() <= 232448 &&
-           (2 * xtma_tile<T, N, V>() * sizeof(T)) % 16 == 0;
+           (2 * xtma_tile<T, N, V>() * sizeof(T)) % 16 == 0 && N % xout_rows<N>() == 0;
 }
 
 template <typename T, int N, int V>
 __global__ void __launch_bounds__(xtma_tile<T, N, V>() * PlansV<N, V>::X::P, xtma_minb<T, N, V>())
-k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ W, const cx<T>* __restrict__ tw,
-           StepDev* __restrict__ sd, const int* __restrict__ xitems, int nvalid, int cnt) {
+k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, const __grid_constant__ CUtensorMap wmap, int cw,
+           const cx<T>* __restrict__ tw, StepDev* __restrict__ sd, const int* __restrict__ xitems, int nvalid, int cnt) {
     using G = Geo<N>;
     using PL = typename PlansV<N, V>::X;
     constexpr int TT = xtma_tile<T, N, V>();
@@ -427,9 +443,12 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
     constexpr int XB = xbox_rows<N>();
     constexpr uint32_t BOX_BYTES = (uint32_t)XB * TT * sizeof(cx<T>);
     extern __shared__ __align__(128) unsigned char smem_raw[];
+    constexpr int SR = xtma_slab_rows<N>();
+    constexpr int XO = xout_rows<N>();
     cx<T>* sbuf = reinterpret_cast<cx<T>*>(smem_raw);       // exchange [N][TT]
-    cx<T>* slab0 = sbuf + (size_t)N * TT;                    // [2][N][TT]
-    uint64_t* bars = reinterpret_cast<uint64_t*>(slab0 + 2 * (size_t)N * TT);
+    cx<T>* obuf = sbuf + (size_t)N * TT;                     // output [N][TT]
+    cx<T>* slab0 = obuf + (size_t)N * TT;                    // [2][SR][TT]
+    uint64_t* bars = reinterpret_cast<uint64_t*>(slab0 + 2 * (size_t)SR * TT);
     const int tid = threadIdx.x;
     const int t = tid % TT, p = tid / TT;
     const int items = nvalid * cnt;
@@ -448,10 +467,10 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
         while (kxm * kxm > r2) --kxm;
         while ((kxm + 1) * (kxm + 1) <= r2) ++kxm;
         const int nb = kxm / XB + 1;   // boxes covering the rows kx = 0 .. kxm
-        cx<T>* dst = slab0 + (size_t)sl * N * TT;
+        cx<T>* dst = slab0 + (size_t)sl * SR * TT;
         const int cc = c0 + 3 * m + c;
         fence_proxy_async_smem();
-        if (2 * nb * XB >= N) {
+        if (SR == N && 2 * nb * XB >= N) {
             mbar_arrive_expect_tx(&bars[sl], (uint32_t)(N / XB) * BOX_BYTES);
             for (int b = 0; b < N / XB; ++b) tensor4_g2s(dst + (size_t)b * XB * TT, &map, 2 * kz0, j, b * XB, cc, &bars[sl]);
         } else {
@@ -459,7 +478,7 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
             for (int b = 0; b < nb; ++b) {
                 const int r_lo = b * XB, r_hi = N - (b + 1) * XB;
                 tensor4_g2s(dst + (size_t)r_lo * TT, &map, 2 * kz0, j, r_lo, cc, &bars[sl]);
-                tensor4_g2s(dst + (size_t)r_hi * TT, &map, 2 * kz0, j, r_hi, cc, &bars[sl]);
+                tensor4_g2s(dst + (size_t)(r_hi - (N - SR)) * TT, &map, 2 * kz0, j, r_hi, cc, &bars[sl]);
             }
         }
     };
@@ -493,6 +512,7 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
             atomicExch(&sd[m].status, kStatusTimeout);
             for (int sl = 0; sl < 2; ++sl)
                 if (pend & (1u << sl)) (void)mbar_wait(&bars[sl], (ph >> sl) & 1u, kWaitCycles);
+            bulk_wait_all();
         }
     };
 
@@ -503,27 +523,37 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
         const int j = ky < 0 ? ky + N : ky;
         const bool colok = (kz <= G::KC) && (ky * ky + kz * kz <= G::KC2);
         const int rem = G::KC2 - ky * ky - kz * kz;
-        const long long off = (long long)j * G::NZP + kz;
-        const long long xs = (long long)N * G::NZP;
-        cx<T>* Wm = W + (long long)m * 6 * G::FS;
         const int nx = it + (int)gridDim.x;
         auto read = [&](int sl, cx<T>(&v)[E]) {
-            const cx<T>* src = slab0 + (size_t)sl * N * TT + t;
+            const cx<T>* src = slab0 + (size_t)sl * SR * TT + t;
 #pragma unroll
             for (int s = 0; s < E; ++s) {
-                const int kx = kof<N>(p + P * s);
-                v[s] = (colok && kx * kx <= rem) ? src[(size_t)(p + P * s) * TT] * scale : czero<T>();
+                const int r = p + P * s;
+                const int kx = kof<N>(r);
+                const bool in = colok && kx * kx <= rem;
+                const int sr = !in ? 0 : (r < N / 2 ? r : r - (N - SR));   // slab row of x row r
+                v[s] = in ? src[(size_t)sr * TT] * scale : czero<T>();
             }
         };
         auto ikx = [&](cx<T>(&v)[E]) {
 #pragma unroll
             for (int s = 0; s < E; ++s) v[s] = mul_i(v[s]) * T(kof<N>(p + P * s));
         };
+        // field f of the tile (every x row, the TT columns; zero outside the circle)
+        // through the output buffer and bulk tensor stores: the buffer is free once
+        // the previous stores have read it
         auto store = [&](int f, const cx<T>(&v)[E]) {
-            if (!colok) return;
-            cx<T>* dst = Wm + (long long)f * G::FS + off;
+            if (tid == 0) bulk_wait_read_all();
+            __syncthreads();
 #pragma unroll
-            for (int s = 0; s < E; ++s) dst[(long long)(p + P * s) * xs] = v[s];
+            for (int s = 0; s < E; ++s) obuf[(size_t)(p + P * s) * TT + t] = v[s];
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                for (int b = 0; b < N / XO; ++b)
+                    tensor4_s2g(&wmap, obuf + (size_t)b * XO * TT, 2 * kz0, j, b * XO, cw + 6 * m + f);
+                bulk_commit();
+            }
         };
         const T fky = T(ky), fkz = T(kz);
         cx<T> X[E], Y[E], B[E];
@@ -582,6 +612,8 @@ k_xinv_tma(const __grid_constant__ CUtensorMap map, int c0, cx<T>* __restrict__ 
         sy = tmp;
         it = nx;
     }
+    // the bulk stores complete before the CTA exits
+    if (tid == 0) bulk_wait_all();
 }
 // ---------------------------------------------------------------------------
 // P2 / P4: FFT along y, in place. grid (ntile, N, nfields).

@@ -79,6 +79,25 @@ __device__ __forceinline__ void tensor4_g2s(void* dst, const CUtensorMap* map, i
         : "memory");
 }
 
+// tiled tensor copy shared -> global of one box of a 4D tensor map at
+// coordinates (c0 innermost .. c3), into the thread's bulk async-group; c0 x
+// element size a multiple of 16 bytes and no coordinate negative (elements
+// beyond the tensor's extent are not written). The shared source is read
+// asynchronously: the writes into it must be ordered before the copy with
+// fence_proxy_async_smem and a barrier.
+__device__ __forceinline__ void tensor4_s2g(const CUtensorMap* map, const void* src, int c0, int c1, int c2, int c3) {
+    asm volatile("cp.async.bulk.tensor.4d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3, %4}], [%5];" ::"l"(
+                     reinterpret_cast<uint64_t>(map)),
+                 "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(src))
+                 : "memory");
+}
+// close the thread's current bulk async-group
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// the thread's bulk async-groups have finished reading their shared sources
+__device__ __forceinline__ void bulk_wait_read_all() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+// the thread's bulk async-groups have completed (writes performed)
+__device__ __forceinline__ void bulk_wait_all() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
+
 // bulk prefetch of global bytes into L2; src 16-byte aligned, bytes % 16 == 0
 __device__ __forceinline__ void bulk_prefetch_l2(const void* src, uint32_t bytes) {
     asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
