@@ -33,3 +33,15 @@ def test_lr_chunks():
     for n in (1, 7, 10, 101, 999):
         assert sum(it for it, _ in b.lr_chunks(n, "step")) == n
         assert all(it > 0 for it, _ in b.lr_chunks(n, "step"))
+
+
+def test_traffic_table():
+    """The committed ncu summary holds the dominant kernel's measured DRAM bytes per launch at
+    the bench's sizes; the 512^3 figure lies between the kernel's written and its read+written
+    compulsory bytes (3 and 9 fields of 512^2 x 176 stored kz rows, FP32 complex)."""
+    b = load_bench()
+    t512 = b.read_traffic("k_zline", 512, "fp32")
+    assert t512 is not None and b.read_traffic("k_zline", 256, "fp32") is not None
+    row = 512 * 512 * 176 * 8
+    assert 3 * row < t512 <= 9 * row
+    assert b.read_traffic("k_zline", 333, "fp32") is None
