@@ -39,6 +39,8 @@ template <typename T, int N, int V = 0>
 class Impl final : public Base {
     using G = Geo<N>;
     using PA = typename Plans<N>::A;
+    using PY = typename YPlan<T, N, true>::A;    // the inverse y pass's plan
+    using PYF = typename YPlan<T, N, false>::A;  // the forward y pass's plan
     using PX = typename PlansV<N, V>::X;
     static constexpr int TA = tile_a<T, N, V>();
     static constexpr int TX = tile_x<T, N, V>();
@@ -247,7 +249,7 @@ class Impl final : public Base {
         k_xinv<T, N, V><<<dim3(NTX, G::NKY, cnt), TX * PX::P, smem_xi(), s_>>>(in + (size_t)m0 * 3 * G::FS, Wm(m0), tw_);
     }
     void p2(int m0, int cnt) {
-        k_ypass<T, N, true, V><<<dim3(NTA, N, 6 * cnt), TA * PA::P, smem_a(), s_>>>(Wm(m0), tw_);
+        k_ypass<T, N, true, V><<<dim3(NTA, N, 6 * cnt), TA * PY::P, smem_a(), s_>>>(Wm(m0), tw_);
     }
     static constexpr size_t smem_zl() { return zline_smem<T, N>(); }
     void p3(int want_umax, int m0, int cnt) {
@@ -290,7 +292,7 @@ class Impl final : public Base {
     int zform() const override { return zform_; }
     int variant() const override { return V; }
     void p4(int m0, int cnt) {
-        k_ypass<T, N, false, V><<<dim3(NTAF, N, 3 * cnt), TAF * PA::P, smem_af(), s_>>>(Wm(m0), tw_);
+        k_ypass<T, N, false, V><<<dim3(NTAF, N, 3 * cnt), TAF * PYF::P, smem_af(), s_>>>(Wm(m0), tw_);
     }
     template <int INTEG, int MODE>
     void p5x(int m0, int cnt, cx<T>* out) {

@@ -40,7 +40,7 @@ def test_rhs_fp64(ns3d, oracle, N):
     assert rel_l2(got, ref) < FP64_TOL
 
 
-@pytest.mark.parametrize("N", [16, 32, 64, 128])
+@pytest.mark.parametrize("N", [16, 32, 64, 96, 128])
 def test_rhs_fp32(ns3d, oracle, N):
     u = dealiased_random(N, N + 1)
     s = ns3d.Solver(N, precision="fp32")
