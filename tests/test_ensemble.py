@@ -87,3 +87,20 @@ def test_group_profile(ns3d):
     with pytest.raises(ns3d.NS3DError):
         ens.profile_group(groups)
     ens.close()
+
+
+def test_ensemble_96_fp32_matches_single_runs(ns3d):
+    """The C4 ensemble's 96^3 FP32 group (the inverse y pass on its 12 x 8 plan of 24
+    elements per thread): two members stepped together equal the same runs stepped alone."""
+    members = [dict(N=96, nu=nu, dt=1e-3, precision="fp32", cfl=0.5) for nu in (0.004, 0.002)]
+    ens = ns3d.Ensemble(members)
+    for i in range(2):
+        ens.InitialConditions(i, "SPECTRUM", seed=21 + i, k0=3.0 + i)
+    ens.step(3)
+    for i, m in enumerate(members):
+        single = ns3d.Solver(**m)
+        single.InitialConditions("SPECTRUM", seed=21 + i, k0=3.0 + i)
+        single.RK4Step(3)
+        assert np.array_equal(ens.get_state(i), single.get_state()), i
+        single.close()
+    ens.close()
